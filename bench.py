@@ -1,0 +1,314 @@
+"""Benchmark of the pyfds GB300 time-stepping path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload acoustic2d|acoustic1d|axi|thermal] [--precision f64|f32|f32_t64]
+
+One benchmark step is one full ``simulate()`` of the workload (default: the
+2048 x 2048 water/steel Acoustic2D field, 4000 time steps, float64). Prints one
+JSON line with Gcell-updates/s: ``value`` with the state resident in HBM (CUDA
+events on the launching stream), ``e2e`` through the public API with host
+buffers (host-to-device inputs and device-to-host outputs inside the timed
+region), the roofline of the step kernel against the measured HBM peak, the CPU
+baseline (the oracle restatement of the reference's scipy step, one replica per
+host core, on a bounded sample) and the SM clocks sampled while timing.
+
+``--impl reference`` times that CPU restatement alone (the reference itself is
+pure Python/scipy and is not shipped): every step is a bounded sample of the same
+workload on all host cores. Under torchrun only rank 0 runs it.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (workload builder, kwargs, bytes per cell-update at f64 / f32 / f32_t64)
+    "acoustic2d": ("acoustic2d_steel_block", {}, {"f64": 64, "f32": 32}),
+    "acoustic1d": ("acoustic1d_water", {}, {"f64": 48, "f32": 24}),
+    "axi": ("axi_disc_source", {}, {"f64": 64, "f32": 32}),
+    "thermal": ("thermal2d_two_materials", {"nt": 2000}, {"f64": 32, "f32": 16, "f32_t64": 24}),
+}
+# CPU sample per process and step of the reference arm (time steps), per workload
+CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 10}
+L2_BYTES = 129 * 2 ** 20
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(key):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summaries."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    pat = re.compile(r"traffic_bytes_per_launch\[%s\]\s*[:=]\s*([0-9.eE+]+)" % re.escape(key))
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, name)) as fh:
+            m = pat.search(fh.read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_sample(wname, steps_per_proc, procs, repeats=1, warmup=0):
+    """Oracle replicas on `procs` host processes; returns (Gcell/s per repeat, cells)."""
+    import multiprocessing as mp
+    from oracle import bench_worker
+    builder, kwargs, _ = WORKLOADS[wname]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=bench_worker.setup, initargs=(builder, kwargs)) as pool:
+        cells = pool.apply(bench_worker.cells)
+        pool.map(bench_worker.run, [1] * procs)  # touch every replica once
+        vals = []
+        for r in range(warmup + repeats):
+            t0 = time.perf_counter()
+            pool.map(bench_worker.run, [steps_per_proc] * procs, chunksize=1)
+            dt = time.perf_counter() - t0
+            if r >= warmup:
+                vals.append(procs * cells * steps_per_proc / dt / 1e9)
+    return vals, cells
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    procs = os.cpu_count() or 1
+    steps = CPU_SAMPLE_STEPS[args.workload]
+    vals, cells = cpu_sample(args.workload, steps, procs, repeats=args.steps, warmup=args.warmup)
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": v, "unit": "Gcell/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": procs * cells * steps / (v * 1e9) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded workload generator)",
+            "config": {"workload": args.workload, "cells": cells, "precision": "f64",
+                       "parallelism": "replicas"},
+            "cpu_baseline": {"value": v, "unit": "Gcell/s", "cores": procs, "kind": "port",
+                             "sample": "%d time steps of the full-size workload per process, "
+                                       "%d processes (one replica each), numpy oracle"
+                                       % (steps, procs)},
+            "e2e": {"value": v, "unit": "Gcell/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    from pyfds_gb300 import workloads, _capi
+    builder, kwargs, balg = WORKLOADS[args.workload]
+    spec = getattr(workloads, builder)(**kwargs)
+    nt = int(spec["steps"])
+    field = workloads.build_field(spec, precision=args.precision)
+    field.assemble_matrices()
+    eng = field._engine()
+    cells = field.num_points
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def zero_state():
+        for name in field._stag_components:
+            for t in eng.buffers[name]:
+                t.zero_()
+            if name in (spec.get("init") or {}):
+                eng.buffers[name][0].copy_(torch.as_tensor(spec["init"][name], device=dev,
+                                                           dtype=eng.buffers[name][0].dtype))
+
+    plan = eng.prepare(0, nt)
+    for _ in range(args.warmup):
+        zero_state()
+        eng.launch(plan)
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            zero_state()
+            eng.launch(plan)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * cells * nt / (ms * 1e-3) / 1e9
+    # step kernel alone: average launch over a timed run without the state reset
+    ev2 = torch.cuda.Event(enable_timing=True)
+    ev3 = torch.cuda.Event(enable_timing=True)
+    zero_state()
+    ev2.record(stream)
+    eng.launch(plan)
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    launch_ms = ev2.elapsed_time(ev3) / nt
+    # ---------------- e2e through the public API with host buffers
+    e2e_steps = max(1, args.steps)
+    host_init = {name: np.zeros(cells) for name in field._stag_components}
+    for name, v in (spec.get("init") or {}).items():
+        host_init[name] = np.array(v, dtype=np.float64)
+    for o in (field.pressure.outputs if hasattr(field, "pressure") else []):
+        o.signals = []
+    h2d = d2h = 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for name in field._stag_components:
+            getattr(field, name).values = host_init[name].copy()
+        field._coef_version += 1  # coefficients count as this step's inputs
+        field.step = 0
+        field.simulate(nt)
+        pot = getattr(field, field._stag_components[0])
+        result = pot.values  # device -> host read of the final potential
+        for o in pot.outputs:
+            o.signals = []
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    last = eng._last
+    tab_bytes = int(last["tabs"]["blob"].numel())
+    coef_bytes = sum(t.numel() * t.element_size() for t in eng.coef_tensors.values())
+    state_bytes = sum(eng.buffers[n][0].numel() * eng.buffers[n][0].element_size()
+                      for n in field._stag_components)
+    out_bytes = sum(o.numel() * 8 for o in last["outs"] if o is not None)
+    h2d = state_bytes + coef_bytes + tab_bytes
+    d2h = out_bytes + result.size * eng.buffers[field._stag_components[0]][0].element_size()
+    e2e_value = ws * cells * nt / e2e_s / 1e9
+    if rank != 0:
+        return 0
+    peak, peak_kind = _peaks()
+    bpc = balg.get(args.precision)
+    achieved = cells * bpc / (launch_ms * 1e-3) / 1e9 if bpc else None
+    traffic = _traffic_from_profiles("%s_%s" % (args.workload, args.precision))
+    line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"f64": "f64", "f32": "f32", "f32_t64": "f32+f64"}[args.precision],
+            "data": "synthetic (seeded workload generator, no dataset)",
+            "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
+                       "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
+                       "precision": args.precision,
+                       "l2": "inputs larger than L2 (working set %.0f MB > %.0f MB)"
+                             % ((state_bytes * 2 + coef_bytes) / 2 ** 20, L2_BYTES / 2 ** 20),
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "stag_step_kernel", "bytes_per_cell": bpc,
+                         "launch_ms": launch_ms},
+            "clocks": clk.summary(),
+            "gpu_launches": int(args.steps * (nt + 1))}
+    if ws == 1 and not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        steps = CPU_SAMPLE_STEPS[args.workload]
+        vals, _ = cpu_sample(args.workload, steps, procs, repeats=1)
+        line["cpu_baseline"] = {"value": vals[0], "unit": "Gcell/s", "cores": procs,
+                                "kind": "port",
+                                "sample": "%d time steps of the full-size workload per process, "
+                                          "%d processes (one replica each), numpy oracle"
+                                          % (steps, procs)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="acoustic2d")
+    ap.add_argument("--precision", choices=["f64", "f32", "f32_t64"], default="f64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

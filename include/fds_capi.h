@@ -1,0 +1,203 @@
+/*
+ * fds_capi.h -- C ABI of libfdsgpu.so, the GB300 engine behind pyfds_gb300.
+ *
+ * The reference (emtpb/pyfds) is pure Python: its hot path is
+ * `Field.simulate()` (pyfds/fields.py:67-95) calling each field's `sim_step()`
+ * (pyfds/acoustics.py:40-52, 111-128, 205-225; pyfds/thermal.py:40-51, 92-107,
+ * 161-176), which applies scipy.sparse DIA operators built by
+ * `assemble_matrices()` and applies boundaries / records outputs
+ * (pyfds/fields.py:591-611, pyfds/regions.py:125-165). This ABI replaces that
+ * loop: one call advances a field by `nsteps` steps on the GPU, with the same
+ * boundary and output semantics, over device buffers the caller owns.
+ *
+ * Conventions
+ *  - Every pointer in these structs is a DEVICE pointer unless stated; the caller
+ *    allocates and owns all memory (PyTorch tensors in pyfds_gb300). The library
+ *    borrows pointers for the duration of a call and retains none.
+ *  - Work is enqueued on `stream` (a cudaStream_t passed as void*; NULL = legacy
+ *    default stream). Calls return after enqueueing; they do not synchronise.
+ *  - Return value: 0 on success, a negative FDS_E* code on failure; the message
+ *    of the last failure on the calling thread is available from fds_last_error.
+ *  - Flat cell index i = x + y * nx (pyfds/fields.py:377); a 1-D field has ny = 1.
+ *    Neighbours are i +- 1 and i +- nx with NO break at row ends: only indices
+ *    outside [0, nx*ny) are dropped, as in the reference's truncated DIA operators.
+ */
+#ifndef FDS_CAPI_H
+#define FDS_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDS_ABI_VERSION 1
+
+/* error codes */
+#define FDS_OK 0
+#define FDS_E_ARG (-1)       /* invalid argument (null pointer, bad size, unknown mode) */
+#define FDS_E_LAUNCH (-2)    /* a CUDA launch or API call failed */
+#define FDS_E_NOKERNEL (-3)  /* no kernel was built for this combination of flags */
+#define FDS_E_TIMEOUT (-4)   /* a bounded device-side wait gave up */
+#define FDS_E_SIZE (-5)      /* a size exceeds a documented maximum */
+
+/* field families (FdsStagProblem.family) */
+#define FDS_FAMILY_ACOUSTIC 0 /* flux components keep memory: v -= (D p - L v) */
+#define FDS_FAMILY_THERMAL 1  /* flux components are overwritten: q = -(D T) */
+
+/* arithmetic (FdsStagProblem.precision) */
+#define FDS_PREC_F64 0     /* all state and coefficients float64 (the drop-in) */
+#define FDS_PREC_F32 1     /* all state and coefficients float32 */
+#define FDS_PREC_F32_T64 2 /* float32 coefficients and fluxes, float64 potential (P/T) */
+
+/* FdsStagProblem.flags */
+#define FDS_FLAG_HAS_V 1u   /* second flux component (2-D fields) */
+#define FDS_FLAG_ABSORB 2u  /* viscous absorption operator present (acoustic) */
+#define FDS_FLAG_AXI 4u     /* axisymmetric: x is the radius (Acoustic3DAxi / Thermal3DAxi) */
+#define FDS_FLAG_EXACT 8u   /* F64 only: reproduce the reference's floating-point
+                              operation order exactly (no fused multiply-add) */
+
+/* Boundary operation flags (FdsBoundOp.flags) */
+#define FDS_BOP_SIGNAL 2 /* value = pool[off + step * stride]  (else value = scalar) */
+
+/*
+ * Per-cell coefficient arrays of one field. Each array has nx*ny entries of the
+ * problem's coefficient type (double for F64, float otherwise) and is indexed by
+ * the cell it multiplies, i.e. by column of the reference's DIA operator
+ * (scipy stores data[k][j] at A[j - offset_k, j]).
+ *
+ *  bx, by : factors of the backward x / y difference that updates the flux
+ *           (reference a_vx_p / a_vy_p: dt/dx/rho; thermal a_qx_t / a_qy_t: kx/dx).
+ *  kx, ky : factors of the forward x / y difference that updates the potential
+ *           (reference a_p_vx / a_p_vy: dt/dx*c^2*rho; thermal a_t_qx / a_t_qy:
+ *           dt/dx/rho/cp). For FDS_FLAG_AXI with FDS_FLAG_EXACT these carry the
+ *           reference's 1/r column factor and the kernel multiplies the flux by r.
+ *  absorption (FDS_FLAG_ABSORB, else NULL): the summed DIA operator
+ *           a_vx_vx = (d_x2 + d_y2 [+ central d_x for AXI]).todia(), as its
+ *           diagonals: aym (offset -nx), axm (offset -1), ad (offset 0),
+ *           axp (offset +1), ayp (offset +nx); each column-indexed.
+ *  ex     : AXI + ABSORB only: dt*mu/rho, the explicit radial loss of
+ *           pyfds/acoustics.py:213-215.
+ *  rx     : AXI only: radius of each column, nx entries (x_j + dx/2).
+ */
+typedef struct FdsCoefs {
+  const void* bx;
+  const void* by;
+  const void* kx;
+  const void* ky;
+  const void* aym;
+  const void* axm;
+  const void* ad;
+  const void* axp;
+  const void* ayp;
+  const void* ex;
+  const void* rx;
+} FdsCoefs;
+
+/* Geometry and variant of one staggered field. */
+typedef struct FdsStagProblem {
+  int32_t family;    /* FDS_FAMILY_* */
+  int32_t precision; /* FDS_PREC_* */
+  uint32_t flags;    /* FDS_FLAG_* */
+  int32_t nx;
+  int32_t ny; /* 1 for 1-D fields */
+  int32_t tile_x; /* tile shape the tables below were built for (fds_stag_tile_shape) */
+  int32_t tile_y;
+  int32_t reserved;
+  FdsCoefs coefs;
+} FdsStagProblem;
+
+/*
+ * Field state, ping-pong buffered. Component 0 is the potential (pressure /
+ * temperature), 1 and 2 the x / y flux (velocity / heat flux). `cur[c]` holds the
+ * current values; `nxt[c]` is scratch of the same size. On return the pointers
+ * are swapped as many times as steps ran, so `cur[c]` again holds the current
+ * values. A thermal flux component may pass cur == nxt (it is never read).
+ */
+typedef struct FdsStagState {
+  void* cur[3];
+  void* nxt[3];
+} FdsStagState;
+
+/* One boundary operation (pyfds/regions.py:125-145):
+ *   new = mul * old + value,
+ * where mul is the boundary's `additive` flag as a number (True -> 1, False -> 0,
+ * as the reference multiplies it in). 32 bytes. */
+typedef struct FdsBoundOp {
+  double scalar;  /* value when !(flags & FDS_BOP_SIGNAL) */
+  double mul;     /* factor of the old value */
+  int64_t off;    /* pool offset of step 0 when FDS_BOP_SIGNAL */
+  int32_t stride; /* pool stride between consecutive steps */
+  int32_t flags;  /* FDS_BOP_* */
+} FdsBoundOp;
+
+/* One boundary cell of one tile: the chain ops[op_begin, op_end) applied in order
+ * to the tile's shared-memory slot `pos`; `cell` is the flat index. 24 bytes. */
+typedef struct FdsBoundGroup {
+  int64_t cell;
+  int32_t pos;
+  int32_t op_begin;
+  int32_t op_end;
+  int32_t pad;
+} FdsBoundGroup;
+
+/* One output sample slot: column `col` of the component's output buffer reads
+ * the tile slot `pos` (flat index `cell`). 16 bytes. */
+typedef struct FdsProbe {
+  int64_t cell;
+  int32_t pos;
+  int32_t col;
+} FdsProbe;
+
+/* Boundary + output tables of one component, bucketed per tile. */
+typedef struct FdsCompTables {
+  const int32_t* bound_tile_start; /* [ntiles + 1] into groups, or NULL if none */
+  const FdsBoundGroup* groups;
+  const FdsBoundOp* ops;
+  const int32_t* probe_tile_start; /* [ntiles + 1] into probes, or NULL if none */
+  const FdsProbe* probes;
+  double* out;  /* [nsteps_capacity, ncols] float64, row = step - step0 */
+  int32_t ncols;
+  int32_t out_rows; /* capacity of `out` in rows */
+} FdsCompTables;
+
+typedef struct FdsStagTables {
+  FdsCompTables comp[3];
+  const double* pool; /* boundary signal values, float64 */
+  int64_t pool_len;
+} FdsStagTables;
+
+/* ABI version of the loaded library (FDS_ABI_VERSION). */
+int32_t fds_abi_version(void);
+
+/* Copies the last error message of the calling thread into buf (NUL-terminated,
+ * truncated to len). Returns the message length. */
+int32_t fds_last_error(char* buf, size_t len);
+
+/* Tile shape (cells in x, y) the kernel for this problem variant uses; host-side
+ * tables must be bucketed for it. Returns FDS_OK or FDS_E_NOKERNEL. */
+int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, int32_t nx,
+                            int32_t ny, int32_t* tile_x, int32_t* tile_y);
+
+/*
+ * Advance one staggered field by `nsteps` steps, steps step0 .. step0+nsteps-1.
+ * Replaces `Field.simulate(nsteps)` (pyfds/fields.py:67-95) of Acoustic1D,
+ * Acoustic2D, Acoustic3DAxi, Thermal1D, Thermal2D and Thermal3DAxi; each step
+ * follows that kind's `sim_step()`:
+ *   potential bounds(step) -> potential outputs -> flux update ->
+ *   x-flux bounds -> x-flux outputs -> y-flux bounds -> y-flux outputs ->
+ *   potential update.
+ * `store_flux` != 0 writes the flux components every step (required for the
+ * acoustic family, whose fluxes carry state); for the thermal family 0 writes
+ * them on the last step only.
+ */
+int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
+                     const FdsStagTables* tables, int64_t step0, int32_t nsteps,
+                     int32_t store_flux, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDS_CAPI_H */

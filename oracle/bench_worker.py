@@ -1,0 +1,45 @@
+"""CPU-baseline worker: runs the oracle's time step on one replica of a workload.
+
+TEST INFRASTRUCTURE: used only by bench.py's CPU-baseline leg and its
+``--impl reference`` arm, through a ``spawn`` process pool (one replica per
+process; the oracle, like the reference's scipy path, is single-threaded).
+"""
+import os
+import time
+
+import numpy as np
+
+from . import fds_oracle as O
+
+_W = {}
+
+
+def setup(workload, kwargs):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from pyfds_gb300 import workloads
+    spec = getattr(workloads, workload)(**kwargs)
+    ops = O.assemble(spec)
+    n = ops["n"]
+    state = {c: np.zeros(n) for c in O.components_of(spec["kind"])}
+    for c, v in (spec.get("init") or {}).items():
+        state[c] = np.array(v, dtype=np.float64)
+    _W.update(spec=spec, ops=ops, state=state, step=0)
+    return os.getpid()
+
+
+def run(nsteps):
+    """Advance this replica by nsteps oracle steps; returns the elapsed seconds."""
+    spec, ops, state = _W["spec"], _W["ops"], _W["state"]
+    outputs = spec.get("outputs") or {}
+    bounds = spec.get("bounds") or {}
+    signals = {c: [[[] for _ in idx] for idx in outputs.get(c, [])]
+               for c in O.components_of(spec["kind"])}
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        O.sim_step(spec["kind"], ops, state, bounds, outputs, signals, _W["step"], dt=spec["dt"])
+        _W["step"] += 1
+    return time.perf_counter() - t0
+
+
+def cells():
+    return int(_W["ops"]["n"])

@@ -1,0 +1,127 @@
+"""Seeded scenario specs for parity tests (test infrastructure only).
+
+A scenario spec is a plain dict understood by ``oracle.fds_oracle.simulate``, by
+``oracle.ref_build.build_reference_field`` (reference, validation only) and by the
+test helpers that build the same field through ``pyfds_gb300``. Every draw uses
+``numpy.random.default_rng(seed)``.
+"""
+import numpy as np
+
+ACOUSTIC_KINDS = ("Acoustic1D", "Acoustic2D", "Acoustic3DAxi")
+THERMAL_KINDS = ("Thermal1D", "Thermal2D", "Thermal3DAxi")
+ALL_KINDS = ACOUSTIC_KINDS + THERMAL_KINDS
+
+
+def _components(kind):
+    from .fds_oracle import components_of
+    return components_of(kind)
+
+
+def _random_material(rng, kind, mu):
+    if kind.startswith("Acoustic"):
+        c = float(rng.uniform(1000, 3000))
+        rho = float(rng.uniform(800, 2000))
+        return {"sound_velocity": c, "density": rho,
+                "absorption_coef": float(rng.uniform(1e-4, 5e-3)) if mu else 0}
+    k = float(rng.uniform(0.2, 200))
+    aniso = rng.random() < 0.5
+    return {"heat_capacity": float(rng.uniform(500, 1500)),
+            "density": float(rng.uniform(1000, 3000)),
+            "thermal_conductivity_x": k,
+            "thermal_conductivity_y": float(rng.uniform(0.2, 200)) if aniso else k}
+
+
+def _pulse(t, f, t0, sigma, amp=1.0):
+    return amp * np.sin(2 * np.pi * f * t) * np.exp(-(t - t0) ** 2 / (2 * sigma ** 2))
+
+
+def random_scenario(seed, kind, nx, ny=None, steps=40, mu=True, boundary_modes="all",
+                    init_noise=True):
+    """A small random scenario that exercises every boundary/output mode.
+
+    - 1..3 extra material regions drawn over random cell subsets (later ones win),
+    - Dirichlet scalar bounds, additive 1-D signals (with duplicate indices),
+      per-point signal lists, 2-D ndarray signals, additive scalars,
+    - outputs on every component, with duplicates,
+    - random initial state so that every stencil term is active from step 0.
+    """
+    rng = np.random.default_rng(seed)
+    is2d = not kind.endswith("1D")
+    ny = (ny or 1) if is2d else 1
+    n = nx * ny
+    dx = 1e-4
+    dy = dx * (float(rng.choice([1.0, 1.25])) if is2d else 1.0)
+    mats = [(None, _random_material(rng, kind, mu))]
+    for _ in range(int(rng.integers(1, 4))):
+        cnt = int(rng.integers(1, max(2, n // 3)))
+        idx = np.sort(rng.choice(n, size=cnt, replace=False))
+        mats.append((idx.tolist(), _random_material(rng, kind, mu)))
+    if kind.startswith("Acoustic"):
+        cmax = max(m[1]["sound_velocity"] for m in mats)
+        dt = 0.4 * min(dx, dy) / cmax / (np.sqrt(2) if is2d else 1.0)
+    else:
+        amax = max(max(m[1]["thermal_conductivity_x"], m[1]["thermal_conductivity_y"])
+                   / (m[1]["density"] * m[1]["heat_capacity"]) for m in mats)
+        dt = 0.2 * min(dx, dy) ** 2 / (4 * amax)
+    nt = steps + 5
+    t = np.arange(nt) * dt
+    comps = _components(kind)
+    bounds = {}
+    outputs = {}
+    f0 = 1.0 / (20 * dt)
+    for ci, comp in enumerate(comps):
+        bl = []
+        modes = ["dirichlet", "signal", "list", "array2d", "scalar_add"]
+        if boundary_modes != "all":
+            modes = list(boundary_modes)
+        for mode in modes:
+            if rng.random() < 0.35 and mode != "dirichlet":
+                continue
+            cnt = int(rng.integers(1, min(6, n) + 1))
+            idx = rng.integers(0, n, size=cnt).tolist()
+            if mode == "dirichlet":
+                # a fixed edge (first/last row or the two ends)
+                if is2d:
+                    edge = list(range(0, nx)) if rng.random() < 0.5 else list(range(0, n, nx))
+                else:
+                    edge = [0, n - 1]
+                bl.append({"indices": edge, "value": float(rng.choice([0.0, 0.5])),
+                           "additive": False})
+            elif mode == "signal":
+                if len(idx) > 1:
+                    idx.append(idx[0])  # duplicate index: fancy assignment, last write wins
+                bl.append({"indices": idx, "value": _pulse(t, f0, 10 * dt, 3 * dt),
+                           "additive": bool(rng.random() < 0.8)})
+            elif mode == "list":
+                sigs = [_pulse(t, f0 * (1 + 0.1 * k), 8 * dt, 2 * dt, amp=1 + k)
+                        for k in range(len(idx))]
+                bl.append({"indices": idx, "value": sigs, "additive": bool(rng.random() < 0.5)})
+            elif mode == "array2d":
+                arr = rng.standard_normal((nt, len(idx))) * 0.1
+                bl.append({"indices": idx, "value": arr, "additive": bool(rng.random() < 0.5)})
+            elif mode == "scalar_add":
+                bl.append({"indices": idx, "value": float(rng.uniform(-0.01, 0.01)),
+                           "additive": True})
+        if bl:
+            bounds[comp] = bl
+        ol = []
+        for _ in range(int(rng.integers(1, 3))):
+            cnt = int(rng.integers(1, min(5, n) + 1))
+            idx = rng.integers(0, n, size=cnt).tolist()
+            if cnt > 1 and rng.random() < 0.3:
+                idx.append(idx[0])
+            ol.append(idx)
+        outputs[comp] = ol
+    init = {}
+    if init_noise:
+        scale = {"pressure": 1.0, "velocity": 1e-6, "velocity_x": 1e-6, "velocity_y": 1e-6,
+                 "temperature": 10.0, "heat_flux": 1.0, "heat_flux_x": 1.0, "heat_flux_y": 1.0}
+        for comp in comps:
+            base = 293.15 if comp == "temperature" else 0.0
+            init[comp] = base + scale[comp] * rng.standard_normal(n)
+    spec = {"kind": kind, "nx": nx, "dx": dx, "dt": dt, "nt": nt, "materials": mats,
+            "bounds": bounds, "outputs": outputs, "init": init, "steps": steps}
+    if is2d:
+        spec["ny"] = ny
+        spec["dy"] = dy
+    return spec

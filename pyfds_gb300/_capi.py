@@ -1,0 +1,140 @@
+"""ctypes binding of libfdsgpu.so (declared in include/fds_capi.h).
+
+The structures below mirror the C declarations field for field; numpy structured
+dtypes mirror the table records so that host-built tables can be uploaded as raw
+bytes. Loading fails loudly when the library has not been built: there is no
+CPU fallback for the time-stepping path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._build import LIB_PATH
+
+FDS_ABI_VERSION = 1
+
+FDS_OK = 0
+FDS_E_ARG = -1
+FDS_E_LAUNCH = -2
+FDS_E_NOKERNEL = -3
+FDS_E_TIMEOUT = -4
+FDS_E_SIZE = -5
+
+FAMILY_ACOUSTIC = 0
+FAMILY_THERMAL = 1
+
+PREC_F64 = 0
+PREC_F32 = 1
+PREC_F32_T64 = 2
+
+FLAG_HAS_V = 1
+FLAG_ABSORB = 2
+FLAG_AXI = 4
+FLAG_EXACT = 8
+
+BOP_SIGNAL = 2
+
+# exported symbols, in header order
+EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape", "fds_stag_run")
+
+
+class FdsCoefs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in
+                ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx")]
+
+
+class FdsStagProblem(C.Structure):
+    _fields_ = [("family", C.c_int32), ("precision", C.c_int32), ("flags", C.c_uint32),
+                ("nx", C.c_int32), ("ny", C.c_int32), ("tile_x", C.c_int32),
+                ("tile_y", C.c_int32), ("reserved", C.c_int32), ("coefs", FdsCoefs)]
+
+
+class FdsStagState(C.Structure):
+    _fields_ = [("cur", C.c_void_p * 3), ("nxt", C.c_void_p * 3)]
+
+
+class FdsCompTables(C.Structure):
+    _fields_ = [("bound_tile_start", C.c_void_p), ("groups", C.c_void_p), ("ops", C.c_void_p),
+                ("probe_tile_start", C.c_void_p), ("probes", C.c_void_p), ("out", C.c_void_p),
+                ("ncols", C.c_int32), ("out_rows", C.c_int32)]
+
+
+class FdsStagTables(C.Structure):
+    _fields_ = [("comp", FdsCompTables * 3), ("pool", C.c_void_p), ("pool_len", C.c_int64)]
+
+
+# numpy mirrors of the table records (sizes asserted against the header's comments)
+BOUND_OP_DTYPE = np.dtype([("scalar", "<f8"), ("mul", "<f8"), ("off", "<i8"),
+                           ("stride", "<i4"), ("flags", "<i4")], align=True)
+BOUND_GROUP_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("op_begin", "<i4"),
+                              ("op_end", "<i4"), ("pad", "<i4")], align=True)
+PROBE_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("col", "<i4")], align=True)
+assert BOUND_OP_DTYPE.itemsize == 32
+assert BOUND_GROUP_DTYPE.itemsize == 24
+assert PROBE_DTYPE.itemsize == 16
+
+
+class FdsError(RuntimeError):
+    """A libfdsgpu.so call failed; carries the library's status code."""
+
+    def __init__(self, code, message):
+        super().__init__("libfdsgpu error %d: %s" % (code, message))
+        self.code = code
+
+
+_lib = None
+
+
+def library_path():
+    return LIB_PATH
+
+
+def load(path=None):
+    """Load (once) and return the CDLL. Raises RuntimeError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "libfdsgpu.so is not built (%s); run `python -c \"import __graft_entry__ as g; "
+            "g.build()\"` or `python -m pyfds_gb300._build`" % path)
+    lib = C.CDLL(path)
+    lib.fds_abi_version.restype = C.c_int32
+    lib.fds_abi_version.argtypes = []
+    lib.fds_last_error.restype = C.c_int32
+    lib.fds_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    lib.fds_stag_tile_shape.restype = C.c_int32
+    lib.fds_stag_tile_shape.argtypes = [C.c_int32, C.c_int32, C.c_uint32, C.c_int32, C.c_int32,
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.fds_stag_run.restype = C.c_int32
+    lib.fds_stag_run.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
+                                 C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_int32,
+                                 C.c_void_p]
+    v = lib.fds_abi_version()
+    if v != FDS_ABI_VERSION:
+        raise RuntimeError("libfdsgpu.so ABI version %d, expected %d (rebuild)" % (v, FDS_ABI_VERSION))
+    _lib = lib
+    return lib
+
+
+def last_error():
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    lib.fds_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code):
+    if code != FDS_OK:
+        raise FdsError(code, last_error())
+    return code
+
+
+def tile_shape(family, precision, flags, nx, ny):
+    lib = load()
+    tx = C.c_int32()
+    ty = C.c_int32()
+    check(lib.fds_stag_tile_shape(family, precision, flags, nx, ny, C.byref(tx), C.byref(ty)))
+    return tx.value, ty.value

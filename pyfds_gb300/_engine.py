@@ -1,0 +1,282 @@
+"""Device side of a staggered field: PyTorch-owned buffers and the C-ABI call.
+
+A field keeps its reference-style host API (``component.values`` as a float64
+numpy array, boundary/output lists); the engine mirrors the state on the GPU,
+uploads what the host changed, compiles the boundary/output tables, calls
+``fds_stag_run`` and turns the device output buffer back into
+``Output.signals`` samples. All device memory is allocated here as torch
+tensors; libfdsgpu.so only borrows the pointers.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from . import _tables
+
+PRECISIONS = {"f64": _capi.PREC_F64, "f32": _capi.PREC_F32, "f32_t64": _capi.PREC_F32_T64}
+
+_ALIGN = 256
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def require_cuda():
+    """The time-stepping path runs on the GPU only: fail loudly without one."""
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyfds_gb300 time stepping needs a CUDA GPU (none is visible); "
+                           "there is no CPU fallback")
+    _capi.load()
+    return torch
+
+
+class _Blob:
+    """Packs host arrays into one device byte buffer (one host-to-device copy)."""
+
+    def __init__(self):
+        self.parts = []
+        self.size = 0
+
+    def add(self, arr):
+        if arr is None:
+            return None
+        b = np.ascontiguousarray(arr).view(np.uint8).reshape(-1)
+        off = self.size
+        self.parts.append((off, b))
+        self.size = (off + b.size + _ALIGN - 1) // _ALIGN * _ALIGN
+        return off
+
+    def upload(self, torch, device):
+        host = np.zeros(max(self.size, _ALIGN), dtype=np.uint8)
+        for off, b in self.parts:
+            host[off:off + b.size] = b
+        dev = torch.from_numpy(host).to(device)
+        return dev
+
+
+class StagEngine:
+    """GPU state, coefficients and tables of one staggered field."""
+
+    def __init__(self, field):
+        self.field = field
+        self.coef_key = None
+        self.coef_tensors = {}
+        self.buffers = {}  # component name -> [cur, nxt] tensors
+        self.table_cache = None
+        self.launches = 0
+
+    # ------------------------------------------------------------------ dtypes
+    def dtypes(self):
+        torch = _torch()
+        prec = self.field.precision
+        if prec == "f64":
+            return torch.float64, torch.float64, torch.float64
+        if prec == "f32":
+            return torch.float32, torch.float32, torch.float32
+        return torch.float64, torch.float32, torch.float32  # f32_t64: potential in float64
+
+    # ------------------------------------------------------------ coefficients
+    def _upload_coefs(self, torch, dev):
+        key = self.field._coef_version
+        if key == self.coef_key:
+            return
+        _, _, tc = self.dtypes()
+        self.coef_tensors = {}
+        for name, arr in self.field._stag_coefs.items():
+            if arr is None:
+                continue
+            self.coef_tensors[name] = torch.from_numpy(
+                np.ascontiguousarray(arr, dtype=np.float64)).to(dev).to(tc)
+        self.coef_key = key
+
+    # ------------------------------------------------------------------- state
+    def _sync_state_to_device(self, torch, dev):
+        tp, tf, _ = self.dtypes()
+        names = self.field._stag_components
+        memory = self.field._stag_family == _capi.FAMILY_ACOUSTIC
+        for k, name in enumerate(names):
+            comp = getattr(self.field, name)
+            dt = tp if k == 0 else tf
+            bufs = self.buffers.get(name)
+            n = self.field.num_points
+            if bufs is None:
+                cur = torch.empty(n, dtype=dt, device=dev)
+                nxt = torch.empty(n, dtype=dt, device=dev) if (k == 0 or memory) else cur
+                bufs = self.buffers[name] = [cur, nxt]
+                comp._attach(self, name)
+                comp._where = "host"
+            if comp._where == "host":
+                vals = np.asarray(comp._values, dtype=np.float64).reshape(-1)
+                if vals.size != n:
+                    raise ValueError("component %s has %d values, field has %d points"
+                                     % (name, vals.size, n))
+                bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
+                comp._where = "both"
+
+    def download(self, name):
+        bufs = self.buffers[name]
+        return bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
+
+    # ------------------------------------------------------------------ tables
+    def _geometry(self):
+        f = self.field
+        prec = PRECISIONS[f.precision]
+        flags = f._stag_flags()
+        tx, ty = _capi.tile_shape(f._stag_family, prec, flags, f._nx, f._ny)
+        return _tables.TileGeometry(f._nx, f._ny, tx, ty, (flags & _capi.FLAG_HAS_V) != 0)
+
+    def _fingerprint(self):
+        parts = []
+        for name in self.field._stag_components:
+            comp = getattr(self.field, name)
+            bp = []
+            for b in comp.boundaries:
+                v = b.value
+                bp.append((id(b), id(b.region), id(b.region.indices), id(v),
+                           float(v) if np.ndim(v) == 0 else np.shape(v) if
+                           isinstance(v, np.ndarray) else len(v), b.additive))
+            op = tuple((id(o), id(o.region), id(o.region.indices)) for o in comp.outputs)
+            parts.append((tuple(bp), op))
+        return tuple(parts)
+
+    def _compile_tables(self, torch, dev, step_end, geo):
+        f = self.field
+        n = f.num_points
+        pool = _tables.SignalPool()
+        comps = []
+        for k, name in enumerate(f._stag_components):
+            comp = getattr(f, name)
+            bt = _tables.compile_bounds(comp.boundaries, n, pool, step_end, geo, k)
+            pt, ncols = _tables.compile_probes(comp.outputs, n, geo)
+            comps.append((bt, pt, ncols))
+        blob = _Blob()
+        offs = []
+        for bt, pt, ncols in comps:
+            o = {}
+            if bt is not None:
+                o["bts"] = blob.add(bt["tile_start"])
+                o["grp"] = blob.add(bt["groups"])
+                o["ops"] = blob.add(bt["ops"])
+            if pt is not None:
+                o["pts"] = blob.add(pt["tile_start"])
+                o["prb"] = blob.add(pt["probes"])
+            offs.append(o)
+        pool_arr = pool.array()
+        pool_off = blob.add(pool_arr)
+        dev_blob = blob.upload(torch, dev)
+        return {"blob": dev_blob, "offs": offs, "ncols": [c[2] for c in comps],
+                "pool_off": pool_off, "pool_len": int(pool_arr.size)}
+
+    def _tables_struct(self, tabs, outs, nsteps):
+        base = tabs["blob"].data_ptr()
+        st = _capi.FdsStagTables()
+        for k in range(3):
+            ct = st.comp[k]
+            if k < len(tabs["offs"]):
+                o = tabs["offs"][k]
+                if "bts" in o:
+                    ct.bound_tile_start = base + o["bts"]
+                    ct.groups = base + o["grp"]
+                    ct.ops = base + o["ops"]
+                if "pts" in o:
+                    ct.probe_tile_start = base + o["pts"]
+                    ct.probes = base + o["prb"]
+                    ct.out = outs[k].data_ptr()
+                    ct.ncols = tabs["ncols"][k]
+                    ct.out_rows = nsteps
+        st.pool = base + tabs["pool_off"]
+        st.pool_len = tabs["pool_len"]
+        return st
+
+    # --------------------------------------------------------------------- run
+    def prepare(self, step0, nsteps, cache_tables=False):
+        """Upload what the host changed and compile the tables for steps
+        ``step0 .. step0+nsteps-1``; returns a launch plan for ``launch``."""
+        torch = require_cuda()
+        f = self.field
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self._upload_coefs(torch, dev)
+        self._sync_state_to_device(torch, dev)
+        geo = self._geometry()
+        step_end = step0 + nsteps
+        if cache_tables:
+            fp = self._fingerprint()
+            if self.table_cache is not None and self.table_cache[0] == fp and \
+                    self.table_cache[2] >= step_end:
+                tabs = self.table_cache[1]
+            else:
+                tabs = self._compile_tables(torch, dev, max(step_end, 1), geo)
+                self.table_cache = (fp, tabs, step_end)
+        else:
+            tabs = self._compile_tables(torch, dev, step_end, geo)
+        outs = [torch.empty((nsteps, max(nc, 1)), dtype=torch.float64, device=dev)
+                if nc else None for nc in tabs["ncols"]]
+        prob = _capi.FdsStagProblem()
+        prob.family = f._stag_family
+        prob.precision = PRECISIONS[f.precision]
+        prob.flags = f._stag_flags()
+        prob.nx = f._nx
+        prob.ny = f._ny
+        prob.tile_x = geo.tx
+        prob.tile_y = geo.ty
+        for name in ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx"):
+            t = self.coef_tensors.get(name)
+            setattr(prob.coefs, name, t.data_ptr() if t is not None else None)
+        return {"prob": prob, "tabs": tabs, "outs": outs,
+                "tstruct": self._tables_struct(tabs, outs, nsteps), "step0": int(step0),
+                "nsteps": int(nsteps), "geo": geo}
+
+    def launch(self, plan):
+        """Enqueue the steps of a plan on the current stream (no host sync)."""
+        torch = _torch()
+        lib = _capi.load()
+        f = self.field
+        names = f._stag_components
+        state = _capi.FdsStagState()
+        for k in range(3):
+            if k < len(names):
+                cur, nxt = self.buffers[names[k]]
+                state.cur[k] = cur.data_ptr()
+                state.nxt[k] = nxt.data_ptr()
+        stream = torch.cuda.current_stream().cuda_stream
+        store_flux = 1 if f._stag_family == _capi.FAMILY_ACOUSTIC else 0
+        code = lib.fds_stag_run(C.byref(plan["prob"]), C.byref(state), C.byref(plan["tstruct"]),
+                                plan["step0"], plan["nsteps"], store_flux, C.c_void_p(stream))
+        _capi.check(code)
+        self.launches += plan["nsteps"]
+        # the call swapped cur/nxt as often as it stepped
+        for k, name in enumerate(names):
+            bufs = self.buffers[name]
+            if state.cur[k] != bufs[0].data_ptr():
+                bufs.reverse()
+            getattr(f, name)._where = "device"
+        self._last = plan  # keeps the tables and output buffers alive
+
+    def finish(self, plan):
+        """Copy the output buffers to the host and append them to Output.signals."""
+        f = self.field
+        for k, name in enumerate(f._stag_components):
+            out_t = plan["outs"][k]
+            if out_t is None:
+                continue
+            host = out_t.to("cpu").numpy()
+            comp = getattr(f, name)
+            for out, c0, npts in _tables.output_column_slices(comp.outputs):
+                block = host[:, c0:c0 + npts]
+                if not out.signals:
+                    out.signals = [list(block[:, j]) for j in range(npts)]
+                else:
+                    for j, sig in enumerate(out.signals[:npts]):
+                        sig.extend(block[:, j])
+
+    def run(self, step0, nsteps, cache_tables=False):
+        """Advance the field by ``nsteps`` steps starting at global step ``step0``."""
+        if nsteps <= 0:
+            return
+        plan = self.prepare(step0, nsteps, cache_tables)
+        self.launch(plan)
+        self.finish(plan)

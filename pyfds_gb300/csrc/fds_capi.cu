@@ -1,0 +1,109 @@
+// C ABI entry points of libfdsgpu.so (declared in include/fds_capi.h).
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "fds_capi.h"
+#include "fds_internal.h"
+
+namespace fds {
+
+static thread_local std::string g_last_error;
+
+int32_t set_error(int32_t code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+static int32_t tile_shape(uint32_t flags, int32_t* tx, int32_t* ty) {
+  if (flags & FDS_FLAG_HAS_V) {
+    *tx = 64;
+    *ty = 16;
+  } else {
+    *tx = 1024;
+    *ty = 1;
+  }
+  return FDS_OK;
+}
+
+}  // namespace fds
+
+extern "C" {
+
+int32_t fds_abi_version(void) { return FDS_ABI_VERSION; }
+
+int32_t fds_last_error(char* buf, size_t len) {
+  const std::string& m = fds::g_last_error;
+  if (buf && len > 0) {
+    size_t k = m.size() < len - 1 ? m.size() : len - 1;
+    memcpy(buf, m.data(), k);
+    buf[k] = '\0';
+  }
+  return (int32_t)m.size();
+}
+
+int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, int32_t nx,
+                            int32_t ny, int32_t* tile_x, int32_t* tile_y) {
+  (void)family;
+  (void)precision;
+  (void)nx;
+  (void)ny;
+  if (!tile_x || !tile_y) return fds::set_error(FDS_E_ARG, "null output pointer");
+  return fds::tile_shape(flags, tile_x, tile_y);
+}
+
+int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
+                     const FdsStagTables* tables, int64_t step0, int32_t nsteps,
+                     int32_t store_flux, void* stream) {
+  using namespace fds;
+  if (!prob || !state || !tables) return set_error(FDS_E_ARG, "null argument");
+  if (prob->nx < 1 || prob->ny < 1) return set_error(FDS_E_ARG, "bad grid %d x %d", prob->nx, prob->ny);
+  if (nsteps < 0 || step0 < 0) return set_error(FDS_E_ARG, "bad step range");
+  const bool has_v = (prob->flags & FDS_FLAG_HAS_V) != 0;
+  if (!has_v && prob->ny != 1) return set_error(FDS_E_ARG, "1-D field needs ny == 1");
+  int32_t tx = 0, ty = 0;
+  tile_shape(prob->flags, &tx, &ty);
+  if (prob->tile_x != tx || prob->tile_y != ty)
+    return set_error(FDS_E_ARG, "tables built for tile %dx%d, kernel uses %dx%d", prob->tile_x,
+                     prob->tile_y, tx, ty);
+  const FdsCoefs& c = prob->coefs;
+  if (!c.bx || !c.kx) return set_error(FDS_E_ARG, "missing coefficient arrays");
+  if ((prob->flags & FDS_FLAG_ABSORB) && (!c.axm || !c.ad || !c.axp || (has_v && (!c.aym || !c.ayp))))
+    return set_error(FDS_E_ARG, "absorption requested without its diagonals");
+  if ((prob->flags & FDS_FLAG_AXI) && !c.rx) return set_error(FDS_E_ARG, "axisymmetric field without radii");
+  if ((prob->flags & FDS_FLAG_AXI) && (prob->flags & FDS_FLAG_ABSORB) && !c.ex)
+    return set_error(FDS_E_ARG, "axisymmetric absorption without its radial loss factor");
+  const int ncomp = has_v ? 3 : 2;
+  for (int k = 0; k < ncomp; ++k)
+    if (!state->cur[k] || !state->nxt[k]) return set_error(FDS_E_ARG, "missing state buffer %d", k);
+  if (prob->family == FDS_FAMILY_ACOUSTIC && !store_flux)
+    return set_error(FDS_E_ARG, "acoustic fluxes carry state: store_flux must be set");
+  for (int k = 0; k < 3; ++k) {
+    const FdsCompTables& t = tables->comp[k];
+    if (t.probe_tile_start && (!t.out || t.out_rows < nsteps))
+      return set_error(FDS_E_ARG, "output buffer of component %d holds %d rows, need %d", k,
+                       t.out_rows, nsteps);
+  }
+  if (nsteps == 0) return FDS_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (prob->precision) {
+    case FDS_PREC_F64:
+      return run_stag_f64(prob, state, tables, step0, nsteps, store_flux, s);
+    case FDS_PREC_F32:
+      if (prob->flags & FDS_FLAG_EXACT) return set_error(FDS_E_ARG, "exact mode is float64 only");
+      return run_stag_f32(prob, state, tables, step0, nsteps, store_flux, s);
+    case FDS_PREC_F32_T64:
+      if (prob->flags & FDS_FLAG_EXACT) return set_error(FDS_E_ARG, "exact mode is float64 only");
+      return run_stag_f32t64(prob, state, tables, step0, nsteps, store_flux, s);
+    default:
+      return set_error(FDS_E_ARG, "unknown precision %d", prob->precision);
+  }
+}
+
+}  // extern "C"

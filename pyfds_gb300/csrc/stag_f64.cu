@@ -1,0 +1,10 @@
+// Float64 instantiations of the fused staggered-grid step (the pyfds drop-in).
+#include "stag_run.cuh"
+
+namespace fds {
+int32_t run_stag_f64(const FdsStagProblem* p, FdsStagState* s, const FdsStagTables* t,
+                     int64_t step0, int32_t nsteps, int32_t store_flux, cudaStream_t st) {
+  return run_stag_typed<double, double, double, true, true>(p, s, t, step0, nsteps, store_flux,
+                                                            st);
+}
+}  // namespace fds

@@ -1,0 +1,87 @@
+"""Host-side table compilation, checked through a NumPy model of the tile kernel
+(tests/helpers.py:KernelModel) that reads the same tables: on small tiles (many
+tiles, partial tiles, row-end wraps at tile seams) it must reproduce the oracle
+bit for bit, for every field kind and boundary/output mode."""
+import numpy as np
+import pytest
+
+from oracle import fds_oracle as O
+from oracle import scenarios as S
+from helpers import KernelModel, build_field
+
+CASES = []
+for seed in range(30):
+    kind = S.ALL_KINDS[seed % 6]
+    if kind.endswith("1D"):
+        CASES.append((seed, kind, [17, 9, 33, 5, 12][seed % 5], None, (4, 1)))
+    else:
+        CASES.append((seed, kind, [9, 7, 5, 11, 8][seed % 5], [7, 6, 9, 4, 5][(seed // 5) % 5],
+                      [(4, 3), (3, 2), (2, 2), (8, 4), (1, 1)][seed % 5]))
+
+
+@pytest.mark.parametrize("seed,kind,nx,ny,tile", CASES)
+def test_kernel_model_matches_oracle(seed, kind, nx, ny, tile):
+    spec = S.random_scenario(seed, kind, nx, ny, steps=6, mu=(seed % 3 != 0))
+    st_o, sg_o = O.simulate(spec, spec["steps"])
+    f = build_field(spec, exact=True)
+    st_m, sg_m = KernelModel(f, tile=tile).run(spec["steps"])
+    for c in st_o:
+        assert np.array_equal(st_o[c], st_m[c]), c
+        for a, b in zip(sg_o[c], sg_m[c]):
+            assert np.array_equal(a, b), c
+
+
+def test_kernel_model_segmented_start_step():
+    spec = S.random_scenario(3, "Acoustic2D", 9, 6, steps=8)
+    st_o, sg_o = O.simulate(spec, spec["steps"])
+    f = build_field(spec, exact=True)
+    m = KernelModel(f, tile=(4, 3))
+    st1, sg1 = m.run(5, step0=0)
+    for c, v in st1.items():
+        getattr(f, c).values = v
+    st2, sg2 = m.run(3, step0=5)
+    for c in st_o:
+        assert np.array_equal(st_o[c], st2[c])
+        for a, b1, b2 in zip(sg_o[c], sg1[c], sg2[c]):
+            assert np.array_equal(a, np.concatenate([b1, b2], axis=1))
+
+
+def test_short_signal_raises_index_error_before_launch():
+    import pyfds_gb300 as fds
+    from pyfds_gb300 import _tables
+    from pyfds_gb300.regions import Region
+    geo = _tables.TileGeometry(6, 5, 4, 3, True)
+    for value in (np.ones(10), np.ones((10, 2)), [np.ones(10), np.ones(10)]):
+        b = fds.Boundary(Region([1, 2]), value=value, additive=True)
+        _tables.compile_bounds([b], 30, _tables.SignalPool(), 10, geo, 0)
+        with pytest.raises(IndexError):
+            _tables.compile_bounds([b], 30, _tables.SignalPool(), 11, geo, 0)
+    # ragged per-point signals: np.ndim raises ValueError, as in Boundary.apply
+    b = fds.Boundary(Region([1, 2]), value=[np.ones(10), np.ones(12)], additive=True)
+    with pytest.raises(ValueError):
+        _tables.compile_bounds([b], 30, _tables.SignalPool(), 10, geo, 0)
+
+
+def test_value_shape_errors():
+    import pyfds_gb300 as fds
+    from pyfds_gb300 import _tables
+    from pyfds_gb300.regions import Region
+    geo = _tables.TileGeometry(6, 5, 4, 3, True)
+    b = fds.Boundary(Region([1, 2, 3]), value=[np.ones(5), np.ones(5)])
+    with pytest.raises(ValueError):
+        _tables.compile_bounds([b], 30, _tables.SignalPool(), 5, geo, 0)
+    b = fds.Boundary(Region([1, 2]), value=[np.ones(5)] * 3)
+    with pytest.raises(IndexError):
+        _tables.compile_bounds([b], 30, _tables.SignalPool(), 5, geo, 0)
+    b = fds.Boundary(Region([1, 2, 99]), value=1.0)
+    with pytest.raises(IndexError):
+        _tables.compile_bounds([b], 30, _tables.SignalPool(), 5, geo, 0)
+
+
+def test_negative_indices_wrap_like_numpy():
+    spec = S.random_scenario(2, "Acoustic1D", 12, None, steps=5, boundary_modes=["dirichlet"])
+    spec["bounds"]["pressure"].append({"indices": [-1, -3], "value": 0.25, "additive": False})
+    st_o, _ = O.simulate(spec, spec["steps"])
+    f = build_field(spec, exact=True)
+    st_m, _ = KernelModel(f, tile=(4, 1)).run(spec["steps"])
+    assert np.array_equal(st_o["pressure"], st_m["pressure"])
