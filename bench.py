@@ -173,9 +173,13 @@ def run_ours(args):
     dev = torch.device("cuda", torch.cuda.current_device())
     from pyfds_gb300 import workloads, _capi
     builder, kwargs, balg = WORKLOADS[args.workload]
+    kwargs = dict(kwargs)
+    if args.time_steps:
+        kwargs["nt"] = args.time_steps
     spec = getattr(workloads, builder)(**kwargs)
     nt = int(spec["steps"])
-    field = workloads.build_field(spec, precision=args.precision)
+    tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else None
+    field = workloads.build_field(spec, precision=args.precision, tile=tile)
     field.assemble_matrices()
     eng = field._engine()
     cells = field.num_points
@@ -226,7 +230,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     launch_ms = ev2.elapsed_time(ev3) / nt
     # ---------------- e2e through the public API with host buffers
-    e2e_steps = max(1, args.steps)
+    e2e_steps = 0 if args.no_e2e else max(1, args.steps)
     host_init = {name: np.zeros(cells) for name in field._stag_components}
     for name, v in (spec.get("init") or {}).items():
         host_init[name] = np.array(v, dtype=np.float64)
@@ -246,7 +250,9 @@ def run_ours(args):
         for o in pot.outputs:
             o.signals = []
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = (time.perf_counter() - t0) / max(e2e_steps, 1)
+    if not e2e_steps:
+        result = np.zeros(0)
     last = eng._last
     tab_bytes = int(last["tabs"]["blob"].numel())
     coef_bytes = sum(t.numel() * t.element_size() for t in eng.coef_tensors.values())
@@ -255,7 +261,7 @@ def run_ours(args):
     out_bytes = sum(o.numel() * 8 for o in last["outs"] if o is not None)
     h2d = state_bytes + coef_bytes + tab_bytes
     d2h = out_bytes + result.size * eng.buffers[field._stag_components[0]][0].element_size()
-    e2e_value = ws * cells * nt / e2e_s / 1e9
+    e2e_value = ws * cells * nt / e2e_s / 1e9 if e2e_steps else None
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -269,7 +275,7 @@ def run_ours(args):
             "data": "synthetic (seeded workload generator, no dataset)",
             "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
-                       "precision": args.precision,
+                       "precision": args.precision, "tile": "%dx%d" % (eng._geometry().tx, eng._geometry().ty),
                        "l2": "inputs larger than L2 (working set %.0f MB > %.0f MB)"
                              % ((state_bytes * 2 + coef_bytes) / 2 ** 20, L2_BYTES / 2 ** 20),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -282,6 +288,8 @@ def run_ours(args):
                          "launch_ms": launch_ms},
             "clocks": clk.summary(),
             "gpu_launches": int(args.steps * (nt + 1))}
+    if args.time_steps:
+        line["config"]["note"] = "time axis shortened for profiling; not a benchmark value"
     if ws == 1 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         steps = CPU_SAMPLE_STEPS[args.workload]
@@ -304,6 +312,10 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="acoustic2d")
     ap.add_argument("--precision", choices=["f64", "f32", "f32_t64"], default="f64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
+    ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
+    ap.add_argument("--time-steps", type=int, default=0,
+                    help="override the workload's time steps per benchmark step (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -102,8 +102,9 @@ typedef struct FdsStagProblem {
   uint32_t flags;    /* FDS_FLAG_* */
   int32_t nx;
   int32_t ny; /* 1 for 1-D fields */
-  int32_t tile_x; /* tile shape the tables below were built for (fds_stag_tile_shape) */
-  int32_t tile_y;
+  int32_t tile_x; /* tile shape the tables below were built for: the default of */
+  int32_t tile_y; /* fds_stag_tile_shape, or for lossless 2-D non-exact variants any
+                     shape listed by fds_stag_tile_menu */
   int32_t reserved;
   FdsCoefs coefs;
 } FdsStagProblem;
@@ -179,6 +180,11 @@ int32_t fds_last_error(char* buf, size_t len);
  * tables must be bucketed for it. Returns FDS_OK or FDS_E_NOKERNEL. */
 int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, int32_t nx,
                             int32_t ny, int32_t* tile_x, int32_t* tile_y);
+
+/* Tile shapes built for the lossless 2-D variants (the autotuner's search space).
+ * Writes up to `capacity` shapes; returns how many exist. (New: no reference
+ * counterpart; tiling is a property of the GPU kernel.) */
+int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t capacity);
 
 /*
  * Advance one staggered field by `nsteps` steps, steps step0 .. step0+nsteps-1.

@@ -36,7 +36,8 @@ FLAG_EXACT = 8
 BOP_SIGNAL = 2
 
 # exported symbols, in header order
-EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape", "fds_stag_run")
+EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
+                    "fds_stag_tile_menu", "fds_stag_run")
 
 
 class FdsCoefs(C.Structure):
@@ -108,6 +109,8 @@ def load(path=None):
     lib.fds_stag_tile_shape.restype = C.c_int32
     lib.fds_stag_tile_shape.argtypes = [C.c_int32, C.c_int32, C.c_uint32, C.c_int32, C.c_int32,
                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.fds_stag_tile_menu.restype = C.c_int32
+    lib.fds_stag_tile_menu.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]
     lib.fds_stag_run.restype = C.c_int32
     lib.fds_stag_run.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                  C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_int32,
@@ -130,6 +133,16 @@ def check(code):
     if code != FDS_OK:
         raise FdsError(code, last_error())
     return code
+
+
+def tile_menu():
+    """Tile shapes (x, y) built for the lossless 2-D variants."""
+    lib = load()
+    n = lib.fds_stag_tile_menu(None, None, 0)
+    xs = (C.c_int32 * n)()
+    ys = (C.c_int32 * n)()
+    lib.fds_stag_tile_menu(xs, ys, n)
+    return [(xs[k], ys[k]) for k in range(n)]
 
 
 def tile_shape(family, precision, flags, nx, ny):

@@ -127,6 +127,9 @@ class StagEngine:
         prec = PRECISIONS[f.precision]
         flags = f._stag_flags()
         tx, ty = _capi.tile_shape(f._stag_family, prec, flags, f._nx, f._ny)
+        tile = getattr(f, "tile", None)
+        if tile is not None and (flags & _capi.FLAG_HAS_V):
+            tx, ty = int(tile[0]), int(tile[1])
         return _tables.TileGeometry(f._nx, f._ny, tx, ty, (flags & _capi.FLAG_HAS_V) != 0)
 
     def _fingerprint(self):

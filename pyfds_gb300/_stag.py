@@ -18,12 +18,14 @@ class StagField:
                  float32 fluxes with a float64 temperature).
       exact:     float64 only; evaluate in the reference's operation order without
                  fused multiply-adds (bit-identical to scipy on x86-64).
+      tile:      (x, y) cells per CTA for lossless 2-D fields, one of
+                 ``_capi.tile_menu()`` (default: the kernel's 64 x 16).
     """
 
     _stag_family = None
     _stag_components = ()
 
-    def _init_gpu(self, precision="f64", exact=False):
+    def _init_gpu(self, precision="f64", exact=False, tile=None):
         if precision not in PRECISIONS:
             raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
         if exact and precision != "f64":
@@ -32,6 +34,7 @@ class StagField:
             raise ValueError("precision='f32_t64' is available for thermal fields only")
         self.precision = precision
         self.exact = bool(exact)
+        self.tile = tuple(tile) if tile is not None else None
         self._stag_coefs = None
         self._flags_base = 0
         self._coef_version = 0

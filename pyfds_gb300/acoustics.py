@@ -26,9 +26,9 @@ class Acoustic1D(_AcousticBase, fld.Field1D):
 
     _stag_components = ('pressure', 'velocity')
 
-    def __init__(self, *args, precision='f64', exact=False, **kwargs):
+    def __init__(self, *args, precision='f64', exact=False, tile=None, **kwargs):
         fld.Field1D.__init__(self, *args, **kwargs)
-        self._init_gpu(precision, exact)
+        self._init_gpu(precision, exact, tile)
         self.pressure = fld.FieldComponent(self.num_points)
         self.velocity = fld.FieldComponent(self.num_points)
 
@@ -70,9 +70,9 @@ class Acoustic2D(_AcousticBase, fld.Field2D):
 
     _stag_components = ('pressure', 'velocity_x', 'velocity_y')
 
-    def __init__(self, *args, precision='f64', exact=False, **kwargs):
+    def __init__(self, *args, precision='f64', exact=False, tile=None, **kwargs):
         fld.Field2D.__init__(self, *args, **kwargs)
-        self._init_gpu(precision, exact)
+        self._init_gpu(precision, exact, tile)
         self.pressure = fld.FieldComponent(self.num_points)
         self.velocity_x = fld.FieldComponent(self.num_points)
         self.velocity_y = fld.FieldComponent(self.num_points)
@@ -139,9 +139,9 @@ class Acoustic3DAxi(_AcousticBase, fld.Field2D):
 
     _stag_components = ('pressure', 'velocity_x', 'velocity_y')
 
-    def __init__(self, *args, precision='f64', exact=False, **kwargs):
+    def __init__(self, *args, precision='f64', exact=False, tile=None, **kwargs):
         fld.Field2D.__init__(self, *args, **kwargs)
-        self._init_gpu(precision, exact)
+        self._init_gpu(precision, exact, tile)
         self.pressure = fld.FieldComponent(self.num_points)
         self.velocity_x = fld.FieldComponent(self.num_points)
         self.velocity_y = fld.FieldComponent(self.num_points)

@@ -58,6 +58,19 @@ int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, i
   return fds::tile_shape(flags, tile_x, tile_y);
 }
 
+int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t capacity) {
+  int32_t k = 0;
+#define FDS_MENU_ENTRY(TX, TY, NT)               \
+  if (tile_x && tile_y && k < capacity) {        \
+    tile_x[k] = TX;                              \
+    tile_y[k] = TY;                              \
+  }                                              \
+  ++k;
+  FDS_TILE_MENU(FDS_MENU_ENTRY)
+#undef FDS_MENU_ENTRY
+  return k;
+}
+
 int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps,
                      int32_t store_flux, void* stream) {
@@ -67,11 +80,8 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
   if (nsteps < 0 || step0 < 0) return set_error(FDS_E_ARG, "bad step range");
   const bool has_v = (prob->flags & FDS_FLAG_HAS_V) != 0;
   if (!has_v && prob->ny != 1) return set_error(FDS_E_ARG, "1-D field needs ny == 1");
-  int32_t tx = 0, ty = 0;
-  tile_shape(prob->flags, &tx, &ty);
-  if (prob->tile_x != tx || prob->tile_y != ty)
-    return set_error(FDS_E_ARG, "tables built for tile %dx%d, kernel uses %dx%d", prob->tile_x,
-                     prob->tile_y, tx, ty);
+  if (prob->tile_x < 1 || prob->tile_y < 1 || (!has_v && prob->tile_y != 1))
+    return set_error(FDS_E_ARG, "bad tile shape %dx%d", prob->tile_x, prob->tile_y);
   const FdsCoefs& c = prob->coefs;
   if (!c.bx || !c.kx) return set_error(FDS_E_ARG, "missing coefficient arrays");
   if ((prob->flags & FDS_FLAG_ABSORB) && (!c.axm || !c.ad || !c.axp || (has_v && (!c.aym || !c.ayp))))

@@ -6,6 +6,11 @@
 
 #include "fds_capi.h"
 
+// Tile shapes (cells x, cells y, threads) built for the lossless 2-D variants: the
+// search space of the host-side autotuner. Every other variant uses the default
+// 64 x 16 (2-D) or 1024 x 1 (1-D) tile.
+#define FDS_TILE_MENU(X) X(64, 16, 256) X(32, 32, 256) X(128, 8, 256) X(64, 32, 512) X(128, 16, 512)
+
 namespace fds {
 
 // Records a printf-style message as the calling thread's last error; returns code.

@@ -10,6 +10,9 @@
 //             U-ext = [x0, x1] x [y0, y1)   (one column right of the tile)
 //             V-ext = [x0, x1) x [y0, y1]   (one row below the tile)
 //             which the potential update of the owned cells reads.
+//   sBx, sKx (and sBy, sKy unless they equal the x factors): the coefficient
+//             tiles, staged with the state so that the FP64 phases read shared
+//             memory only (no global-load latency between fused multiply-adds).
 //
 // Every slot is addressed by the flat index i = x + y*nx of its (x, y), so the
 // reference's row-end wrap (cell (nx-1, y) couples to (0, y+1)) and the dropping
@@ -66,6 +69,7 @@ struct StagArgs {
   int64_t step0;
   int32_t apply_next;
   int32_t store_flux;
+  int32_t iso;  // by == bx and ky == kx: the y factors are not staged separately
 };
 
 // Variant switches of the tile kernel.
@@ -84,6 +88,7 @@ struct StagCfg {
   static constexpr int RX = TX + 3;
   static constexpr int RY = HAS_V ? TY + 3 : TY;
   static constexpr int RN = RX * RY;
+  static constexpr int MIN_BLOCKS = HAS_V ? (NT >= 512 ? 2 : 4) : 2;
 };
 
 template <typename T>
@@ -160,15 +165,13 @@ __device__ __forceinline__ TF absorb_fma(const StagArgs<TP, TF, TC>& a, const TF
 }
 
 // New flux at flat index i from the potential slots (pos, pos - back) and the
-// old flux. `b`/`bm` are the factors of this cell and of the backward neighbour.
+// old flux; sB holds this direction's factors (slots of out-of-range cells hold 0).
 template <class C, bool IS_X, typename TP, typename TF, typename TC>
 __device__ __forceinline__ TF flux_new(const StagArgs<TP, TF, TC>& a, const TP* sP, const TF* sF,
-                                       int pos, int64_t i, int x) {
+                                       const TC* sB, int pos, int64_t i, int x) {
   const int back = IS_X ? 1 : C::RX;
-  const int64_t ib = i - (IS_X ? 1 : a.nx);
-  const TC* bcoef = IS_X ? a.bx : a.by;
-  const TF b = (TF)__ldg(bcoef + i);
-  const TF bm = (TF)ldg0(bcoef, ib, a.n);
+  const TF b = (TF)sB[pos];
+  const TF bm = (TF)sB[pos - back];
   const TF p = (TF)sP[pos];
   const TF pm = (TF)sP[pos - back];
   if constexpr (C::EXACT) {
@@ -205,12 +208,26 @@ __device__ __forceinline__ TF flux_new(const StagArgs<TP, TF, TC>& a, const TP* 
   }
 }
 
+// Dynamic shared memory of one CTA of this variant.
 template <class C, typename TP, typename TF, typename TC>
-__global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF, TC> a) {
+constexpr size_t stag_smem_bytes(bool iso) {
+  return (size_t)C::RN * (sizeof(TP) + (C::HAS_V ? 2 : 1) * sizeof(TF) +
+                          (iso || !C::HAS_V ? 2 : 4) * sizeof(TC));
+}
+
+template <class C, typename TP, typename TF, typename TC>
+__global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
+    stag_step_kernel(const StagArgs<TP, TF, TC> a) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, RN = C::RN, OY = C::OY;
-  __shared__ TP sP[RN];
-  __shared__ TF sU[RN];
-  __shared__ TF sV[C::HAS_V ? RN : 1];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TP* sP = reinterpret_cast<TP*>(smem_raw);
+  TF* sU = reinterpret_cast<TF*>(sP + RN);
+  TF* sV = sU + (C::HAS_V ? RN : 0);
+  TC* sBx = reinterpret_cast<TC*>(sV + RN);
+  TC* sKx = sBx + RN;
+  const bool iso = a.iso || !C::HAS_V;
+  TC* sBy = iso ? sBx : sKx + RN;
+  TC* sKy = iso ? sKx : sBy + RN;
 
   const int tile = blockIdx.x;
   const int tx = tile % a.tiles_x;
@@ -221,7 +238,7 @@ __global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF,
   const int y1 = min(y0 + TY, a.ny);
   const int tid = threadIdx.x;
 
-  // ---- stage the potential (and old flux) over the region ----
+  // ---- stage the potential, old flux and coefficients over the region ----
   for (int e = tid; e < RN; e += NT) {
     const int lx = e % RX - 1;
     const int ly = e / RX - OY;
@@ -231,6 +248,12 @@ __global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF,
     if constexpr (C::MEMORY) {
       sU[e] = ok ? a.u_in[f] : TF(0);
       if constexpr (C::HAS_V) sV[e] = ok ? a.v_in[f] : TF(0);
+    }
+    sBx[e] = ok ? __ldg(a.bx + f) : TC(0);
+    sKx[e] = ok ? __ldg(a.kx + f) : TC(0);
+    if (!iso) {
+      sBy[e] = ok ? __ldg(a.by + f) : TC(0);
+      sKy[e] = ok ? __ldg(a.ky + f) : TC(0);
     }
   }
   __syncthreads();
@@ -255,7 +278,7 @@ __global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF,
       if (x <= x1 && y < y1 && f < a.n) {
         const int pos = (ly + OY) * RX + lx + 1;
         const int xr = (x == a.nx) ? 0 : x;  // column of the wrapped halo cell
-        un[k] = flux_new<C, true>(a, sP, sU, pos, f, xr);
+        un[k] = flux_new<C, true>(a, sP, sU, sBx, pos, f, xr);
       }
     }
   }
@@ -272,7 +295,7 @@ __global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF,
         const int64_t f = (int64_t)y * a.nx + x;
         if (x < x1 && y <= y1 && f < a.n) {
           const int pos = (ly + OY) * RX + lx + 1;
-          vn[k] = flux_new<C, false>(a, sP, sV, pos, f, x);
+          vn[k] = flux_new<C, false>(a, sP, sV, sBy, pos, f, x);
         }
       }
     }
@@ -318,14 +341,14 @@ __global__ void __launch_bounds__(C::NT) stag_step_kernel(const StagArgs<TP, TF,
         a.u_out[f] = sU[pos];
         if constexpr (C::HAS_V) a.v_out[f] = sV[pos];
       }
-      const TF kxi = (TF)__ldg(a.kx + f);
-      const TF kxn = (TF)ldg0(a.kx, f + 1, a.n);
+      const TF kxi = (TF)sKx[pos];
+      const TF kxn = (TF)sKx[pos + 1];
       const TF u = sU[pos];
       const TF un1 = sU[pos + 1];
       TF kyi = TF(0), kyn = TF(0), v = TF(0), vn1 = TF(0);
       if constexpr (C::HAS_V) {
-        kyi = (TF)__ldg(a.ky + f);
-        kyn = (TF)ldg0(a.ky, f + a.nx, a.n);
+        kyi = (TF)sKy[pos];
+        kyn = (TF)sKy[pos + RX];
         v = sV[pos];
         vn1 = sV[pos + RX];
       }

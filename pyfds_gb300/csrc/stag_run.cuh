@@ -18,12 +18,21 @@ using StagLaunch = void (*)(const StagArgs<TP, TF, TC>&, int, cudaStream_t);
 
 template <class C, typename TP, typename TF, typename TC>
 void launch_stag(const StagArgs<TP, TF, TC>& a, int ntiles, cudaStream_t s) {
-  stag_step_kernel<C, TP, TF, TC><<<ntiles, C::NT, 0, s>>>(a);
+  const size_t smem = stag_smem_bytes<C, TP, TF, TC>(a.iso != 0);
+  static bool attr_set = false;  // opt in once per kernel variant (largest size)
+  if (!attr_set) {
+    cudaFuncSetAttribute(stag_step_kernel<C, TP, TF, TC>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)stag_smem_bytes<C, TP, TF, TC>(false));
+    attr_set = true;
+  }
+  stag_step_kernel<C, TP, TF, TC><<<ntiles, C::NT, smem, s>>>(a);
 }
 
-// Kernel of one variant; nullptr when not built for this precision.
+// Kernel of one variant; nullptr when not built for this precision or tile.
 template <typename TP, typename TF, typename TC, bool ALLOW_EXACT, bool ALLOW_ACOUSTIC>
-StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, bool exact) {
+StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, bool exact,
+                                 int tx, int ty) {
   constexpr int T = kThreads;
   const bool acoustic = (family == FDS_FAMILY_ACOUSTIC);
   if (exact && !ALLOW_EXACT) return nullptr;
@@ -32,13 +41,23 @@ StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, 
   // the radius only enters the kernel through the exact pressure scaling and the
   // radial loss term; otherwise the axisymmetric step is the planar one
   if (axi && !exact && !absorb) axi = false;
-#define FDS_PICK(TX, TY, HV, MEM, ABS, AX, EX)                                         \
-  if (has_v == HV && acoustic == MEM && absorb == ABS && axi == AX && exact == EX)     \
+  const bool dflt = has_v ? (tx == kTile2dX && ty == kTile2dY) : (tx == kTile1dX && ty == 1);
+#define FDS_PICK(TX, TY, HV, MEM, ABS, AX, EX)                                              \
+  if (dflt && has_v == HV && acoustic == MEM && absorb == ABS && axi == AX && exact == EX) \
     return &launch_stag<StagCfg<TX, TY, T, HV, MEM, ABS, AX, EX>, TP, TF, TC>;
+#define FDS_PICK_TILE(TX, TY, NT)                                                            \
+  if (has_v && !absorb && !axi && !exact && tx == TX && ty == TY) {                          \
+    if (acoustic) {                                                                          \
+      if constexpr (ALLOW_ACOUSTIC)                                                          \
+        return &launch_stag<StagCfg<TX, TY, NT, true, true, false, false, false>, TP, TF, TC>; \
+    } else {                                                                                 \
+      return &launch_stag<StagCfg<TX, TY, NT, true, false, false, false, false>, TP, TF, TC>;  \
+    }                                                                                        \
+  }
+  FDS_TILE_MENU(FDS_PICK_TILE)
   if constexpr (ALLOW_ACOUSTIC) {
     FDS_PICK(kTile1dX, 1, false, true, false, false, false)
     FDS_PICK(kTile1dX, 1, false, true, true, false, false)
-    FDS_PICK(kTile2dX, kTile2dY, true, true, false, false, false)
     FDS_PICK(kTile2dX, kTile2dY, true, true, true, false, false)
     FDS_PICK(kTile2dX, kTile2dY, true, true, true, true, false)
     if constexpr (ALLOW_EXACT) {
@@ -51,13 +70,13 @@ StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, 
     }
   }
   FDS_PICK(kTile1dX, 1, false, false, false, false, false)
-  FDS_PICK(kTile2dX, kTile2dY, true, false, false, false, false)
   if constexpr (ALLOW_EXACT) {
     FDS_PICK(kTile1dX, 1, false, false, false, false, true)
     FDS_PICK(kTile2dX, kTile2dY, true, false, false, false, true)
     FDS_PICK(kTile2dX, kTile2dY, true, false, false, true, true)
   }
 #undef FDS_PICK
+#undef FDS_PICK_TILE
   return nullptr;
 }
 
@@ -69,9 +88,12 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   const bool axi = (prob->flags & FDS_FLAG_AXI) != 0;
   const bool exact = (prob->flags & FDS_FLAG_EXACT) != 0;
   StagLaunch<TP, TF, TC> fn =
-      pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi, exact);
-  if (!fn) return set_error(FDS_E_NOKERNEL, "no kernel built for family=%d precision=%d flags=%u",
-                            prob->family, prob->precision, prob->flags);
+      pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi, exact,
+                                                         prob->tile_x, prob->tile_y);
+  if (!fn)
+    return set_error(FDS_E_NOKERNEL,
+                     "no kernel built for family=%d precision=%d flags=%u tile=%dx%d",
+                     prob->family, prob->precision, prob->flags, prob->tile_x, prob->tile_y);
   const int tiles_x = (prob->nx + prob->tile_x - 1) / prob->tile_x;
   const int tiles_y = (prob->ny + prob->tile_y - 1) / prob->tile_y;
   const int64_t ntiles64 = (int64_t)tiles_x * tiles_y;
@@ -95,6 +117,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   a.ayp = (const TC*)c.ayp;
   a.ex = (const TC*)c.ex;
   a.rx = (const TC*)c.rx;
+  a.iso = (a.by == a.bx && a.ky == a.kx) ? 1 : 0;
   for (int k = 0; k < 3; ++k) a.tab[k] = tabs->comp[k];
   a.pool = tabs->pool;
   a.step0 = step0;

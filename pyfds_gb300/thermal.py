@@ -20,9 +20,9 @@ class Thermal1D(StagField, fld.Field1D):
     _stag_family = _capi.FAMILY_THERMAL
     _stag_components = ('temperature', 'heat_flux')
 
-    def __init__(self, *args, precision='f64', exact=False, **kwargs):
+    def __init__(self, *args, precision='f64', exact=False, tile=None, **kwargs):
         fld.Field1D.__init__(self, *args, **kwargs)
-        self._init_gpu(precision, exact)
+        self._init_gpu(precision, exact, tile)
         self.temperature = fld.FieldComponent(self.num_points)
         self.heat_flux = fld.FieldComponent(self.num_points)
 
@@ -53,9 +53,9 @@ class Thermal2D(StagField, fld.Field2D):
     _stag_family = _capi.FAMILY_THERMAL
     _stag_components = ('temperature', 'heat_flux_x', 'heat_flux_y')
 
-    def __init__(self, *args, precision='f64', exact=False, **kwargs):
+    def __init__(self, *args, precision='f64', exact=False, tile=None, **kwargs):
         fld.Field2D.__init__(self, *args, **kwargs)
-        self._init_gpu(precision, exact)
+        self._init_gpu(precision, exact, tile)
         self.temperature = fld.FieldComponent(self.num_points)
         self.heat_flux_x = fld.FieldComponent(self.num_points)
         self.heat_flux_y = fld.FieldComponent(self.num_points)

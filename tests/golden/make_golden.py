@@ -38,6 +38,7 @@ from oracle.fds_oracle import components_of  # noqa: E402
 from pyfds_gb300 import workloads  # noqa: E402
 sys.path.insert(0, os.path.dirname(HERE))
 from golden_digest import spec_digest  # noqa: E402
+from golden_inputs import pack_inputs  # noqa: E402
 
 RANDOM_CASES = []
 for _seed in range(36):
@@ -50,7 +51,8 @@ for _seed in range(36):
                          "mu": _seed % 3 != 0})
 
 
-def run_and_pack(spec, prefix, out, keep_state=True, steps=None):
+def run_and_pack(spec, prefix, out, keep_state=True, steps=None, materials=False):
+    pack_inputs(spec, out, prefix, materials=materials)
     state, sig = ref_build.run_reference(spec, steps or spec["steps"])
     for c in components_of(spec["kind"]):
         if keep_state:
@@ -96,7 +98,7 @@ def make_random():
                                          steps=case["steps"], mu=case["mu"])
         prefix = "s%d/" % case["seed"]
         out[prefix + "digest"] = np.array(spec_digest(spec))
-        run_and_pack(spec, prefix, out)
+        run_and_pack(spec, prefix, out, materials=True)
     out["cases"] = np.array(json.dumps(RANDOM_CASES))
     np.savez_compressed(os.path.join(HERE, "random_scenarios.npz"), **out)
 

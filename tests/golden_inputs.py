@@ -1,0 +1,63 @@
+"""Platform-independent fixture inputs.
+
+Source pulses (np.sin / np.exp), seeded normal draws and index sets derived from
+transcendental functions can differ by an ulp between the machine that generated
+a fixture and the one that checks it. Fixtures therefore carry every such input
+array exactly as the reference consumed it; ``apply_inputs`` puts them back into a
+freshly generated spec before a run.
+"""
+import numpy as np
+
+
+def pack_inputs(spec, out, prefix="", materials=False):
+    """Store the float inputs of ``spec`` (and, if asked, its material index sets).
+
+    Index sets of the workload generators are integer arithmetic or thresholds of a
+    sine far from integer rows, so they do not depend on the platform; constant
+    initial states are stored as one value."""
+    if materials:
+        for k, (idx, _) in enumerate(spec["materials"]):
+            if idx is not None:
+                out[prefix + "in/mat/%d" % k] = np.asarray(idx, dtype=np.int64)
+    for name, v in (spec.get("init") or {}).items():
+        v = np.asarray(v, dtype=np.float64)
+        if v.size and np.all(v == v.reshape(-1)[0]):
+            out[prefix + "in/initc/" + name] = np.array([v.size, v.reshape(-1)[0]])
+        else:
+            out[prefix + "in/init/" + name] = v
+    for name, blist in (spec.get("bounds") or {}).items():
+        for j, b in enumerate(blist):
+            v = b["value"]
+            if np.ndim(v) == 0:
+                continue
+            if isinstance(v, np.ndarray):
+                out[prefix + "in/bound/%s/%d/array" % (name, j)] = v
+            else:
+                out[prefix + "in/bound/%s/%d/list" % (name, j)] = np.stack(
+                    [np.asarray(s, dtype=np.float64) for s in v])
+
+
+def apply_inputs(spec, g, prefix=""):
+    keys = set(g.files)
+    mats = []
+    for k, (idx, params) in enumerate(spec["materials"]):
+        key = prefix + "in/mat/%d" % k
+        mats.append((g[key] if key in keys else idx, params))
+    spec["materials"] = mats
+    for name in list((spec.get("init") or {}).keys()):
+        key = prefix + "in/init/" + name
+        keyc = prefix + "in/initc/" + name
+        if key in keys:
+            spec["init"][name] = g[key]
+        elif keyc in keys:
+            n, v = g[keyc]
+            spec["init"][name] = np.full(int(n), v)
+    for name, blist in (spec.get("bounds") or {}).items():
+        for j, b in enumerate(blist):
+            ka = prefix + "in/bound/%s/%d/array" % (name, j)
+            kl = prefix + "in/bound/%s/%d/list" % (name, j)
+            if ka in keys:
+                b["value"] = g[ka]
+            elif kl in keys:
+                b["value"] = [row for row in g[kl]]
+    return spec
