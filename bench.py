@@ -180,6 +180,7 @@ def run_ours(args):
     nt = int(spec["steps"])
     tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else None
     field = workloads.build_field(spec, precision=args.precision, tile=tile)
+    field.stages = args.stages
     field.assemble_matrices()
     eng = field._engine()
     cells = field.num_points
@@ -276,6 +277,7 @@ def run_ours(args):
             "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
                        "precision": args.precision, "tile": "%dx%d" % (eng._geometry().tx, eng._geometry().ty),
+                       "stages": args.stages,
                        "l2": "inputs larger than L2 (working set %.0f MB > %.0f MB)"
                              % ((state_bytes * 2 + coef_bytes) / 2 ** 20, L2_BYTES / 2 ** 20),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -314,6 +316,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
+    ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2],
+                    help="staging buffers per CTA (0: automatic)")
     ap.add_argument("--time-steps", type=int, default=0,
                     help="override the workload's time steps per benchmark step (profiling)")
     args = ap.parse_args()

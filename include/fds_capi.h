@@ -105,7 +105,8 @@ typedef struct FdsStagProblem {
   int32_t tile_x; /* tile shape the tables below were built for: the default of */
   int32_t tile_y; /* fds_stag_tile_shape, or for lossless 2-D non-exact variants any
                      shape listed by fds_stag_tile_menu */
-  int32_t reserved;
+  int32_t stages; /* 0: automatic; 1: one CTA per tile; 2: persistent CTAs that prefetch
+                     the next tile while computing one (lossless 2-D variants) */
   FdsCoefs coefs;
 } FdsStagProblem;
 
@@ -167,7 +168,13 @@ typedef struct FdsStagTables {
   FdsCompTables comp[3];
   const double* pool; /* boundary signal values, float64 */
   int64_t pool_len;
+  int32_t* status;    /* device int32 the kernels OR FDS_STATUS_* bits into, or NULL;
+                         the caller zeroes it and reads it after the stream work */
 } FdsStagTables;
+
+/* Bits of FdsStagTables.status */
+#define FDS_STATUS_TMA_TIMEOUT 1 /* a tile's TMA copies did not land within the
+                                    bounded wait; that tile was not updated */
 
 /* ABI version of the loaded library (FDS_ABI_VERSION). */
 int32_t fds_abi_version(void);
@@ -182,9 +189,13 @@ int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, i
                             int32_t ny, int32_t* tile_x, int32_t* tile_y);
 
 /* Tile shapes built for the lossless 2-D variants (the autotuner's search space).
- * Writes up to `capacity` shapes; returns how many exist. (New: no reference
- * counterpart; tiling is a property of the GPU kernel.) */
-int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t capacity);
+ * Writes up to `capacity` entries; returns how many exist. `layout` tells how the
+ * host numbers the slots of a tile in FdsBoundGroup.pos / FdsProbe.pos:
+ *   0 (shared-memory tile): pos = (ly + 1) * (tile_x + 8) + lx + 4   (1-D: ly + 0)
+ *   1 (register marching):  pos = ly * (tile_x + 2) + lx + 1
+ * with (lx, ly) the cell relative to the tile's first owned cell. (New: no
+ * reference counterpart; tiling is a property of the GPU kernel.) */
+int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, int32_t capacity);
 
 /*
  * Advance one staggered field by `nsteps` steps, steps step0 .. step0+nsteps-1.

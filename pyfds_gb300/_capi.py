@@ -48,7 +48,7 @@ class FdsCoefs(C.Structure):
 class FdsStagProblem(C.Structure):
     _fields_ = [("family", C.c_int32), ("precision", C.c_int32), ("flags", C.c_uint32),
                 ("nx", C.c_int32), ("ny", C.c_int32), ("tile_x", C.c_int32),
-                ("tile_y", C.c_int32), ("reserved", C.c_int32), ("coefs", FdsCoefs)]
+                ("tile_y", C.c_int32), ("stages", C.c_int32), ("coefs", FdsCoefs)]
 
 
 class FdsStagState(C.Structure):
@@ -62,7 +62,11 @@ class FdsCompTables(C.Structure):
 
 
 class FdsStagTables(C.Structure):
-    _fields_ = [("comp", FdsCompTables * 3), ("pool", C.c_void_p), ("pool_len", C.c_int64)]
+    _fields_ = [("comp", FdsCompTables * 3), ("pool", C.c_void_p), ("pool_len", C.c_int64),
+                ("status", C.c_void_p)]
+
+
+STATUS_TMA_TIMEOUT = 1
 
 
 # numpy mirrors of the table records (sizes asserted against the header's comments)
@@ -110,7 +114,8 @@ def load(path=None):
     lib.fds_stag_tile_shape.argtypes = [C.c_int32, C.c_int32, C.c_uint32, C.c_int32, C.c_int32,
                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     lib.fds_stag_tile_menu.restype = C.c_int32
-    lib.fds_stag_tile_menu.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32]
+    lib.fds_stag_tile_menu.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32), C.c_int32]
     lib.fds_stag_run.restype = C.c_int32
     lib.fds_stag_run.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                  C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_int32,
@@ -135,14 +140,26 @@ def check(code):
     return code
 
 
-def tile_menu():
-    """Tile shapes (x, y) built for the lossless 2-D variants."""
+def tile_menu(with_layout=False):
+    """Tile shapes (x, y) built for the lossless 2-D variants; with ``with_layout``
+    (x, y, layout): 0 = shared-memory tile, 1 = register-marching warp strip."""
     lib = load()
-    n = lib.fds_stag_tile_menu(None, None, 0)
+    n = lib.fds_stag_tile_menu(None, None, None, 0)
     xs = (C.c_int32 * n)()
     ys = (C.c_int32 * n)()
-    lib.fds_stag_tile_menu(xs, ys, n)
+    ls = (C.c_int32 * n)()
+    lib.fds_stag_tile_menu(xs, ys, ls, n)
+    if with_layout:
+        return [(xs[k], ys[k], ls[k]) for k in range(n)]
     return [(xs[k], ys[k]) for k in range(n)]
+
+
+def tile_layout(tx, ty):
+    """Slot layout of a tile shape (0 for every shape outside the menu)."""
+    for x, y, lay in tile_menu(with_layout=True):
+        if (x, y) == (tx, ty):
+            return lay
+    return 0
 
 
 def tile_shape(family, precision, flags, nx, ny):

@@ -68,6 +68,7 @@ class StagEngine:
         self.buffers = {}  # component name -> [cur, nxt] tensors
         self.table_cache = None
         self.launches = 0
+        self.status = None  # device int32: FDS_STATUS_* bits reported by the kernels
 
     # ------------------------------------------------------------------ dtypes
     def dtypes(self):
@@ -130,7 +131,9 @@ class StagEngine:
         tile = getattr(f, "tile", None)
         if tile is not None and (flags & _capi.FLAG_HAS_V):
             tx, ty = int(tile[0]), int(tile[1])
-        return _tables.TileGeometry(f._nx, f._ny, tx, ty, (flags & _capi.FLAG_HAS_V) != 0)
+        layout = _capi.tile_layout(tx, ty) if (flags & _capi.FLAG_HAS_V) else 0
+        return _tables.TileGeometry(f._nx, f._ny, tx, ty, (flags & _capi.FLAG_HAS_V) != 0,
+                                    layout)
 
     def _fingerprint(self):
         parts = []
@@ -226,12 +229,16 @@ class StagEngine:
         prob.ny = f._ny
         prob.tile_x = geo.tx
         prob.tile_y = geo.ty
+        prob.stages = int(getattr(f, "stages", 0) or 0)
         for name in ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx"):
             t = self.coef_tensors.get(name)
             setattr(prob.coefs, name, t.data_ptr() if t is not None else None)
-        return {"prob": prob, "tabs": tabs, "outs": outs,
-                "tstruct": self._tables_struct(tabs, outs, nsteps), "step0": int(step0),
-                "nsteps": int(nsteps), "geo": geo}
+        if self.status is None:
+            self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        tstruct = self._tables_struct(tabs, outs, nsteps)
+        tstruct.status = self.status.data_ptr()
+        return {"prob": prob, "tabs": tabs, "outs": outs, "tstruct": tstruct,
+                "step0": int(step0), "nsteps": int(nsteps), "geo": geo}
 
     def launch(self, plan):
         """Enqueue the steps of a plan on the current stream (no host sync)."""
@@ -260,8 +267,15 @@ class StagEngine:
         self._last = plan  # keeps the tables and output buffers alive
 
     def finish(self, plan):
-        """Copy the output buffers to the host and append them to Output.signals."""
+        """Copy the output buffers to the host and append them to Output.signals;
+        raise if a kernel reported a failed bounded wait."""
         f = self.field
+        st = int(self.status.item())
+        if st:
+            self.status.zero_()
+            raise _capi.FdsError(_capi.FDS_E_TIMEOUT,
+                                 "a kernel reported status 0x%x (TMA copies did not land within "
+                                 "the bounded wait); the field state is not valid" % st)
         for k, name in enumerate(f._stag_components):
             out_t = plan["outs"][k]
             if out_t is None:

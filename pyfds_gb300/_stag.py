@@ -35,6 +35,7 @@ class StagField:
         self.precision = precision
         self.exact = bool(exact)
         self.tile = tuple(tile) if tile is not None else None
+        self.stages = 0  # 0: automatic; 1 or 2 staging buffers (see FdsStagProblem)
         self._stag_coefs = None
         self._flags_base = 0
         self._coef_version = 0

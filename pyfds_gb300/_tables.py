@@ -25,16 +25,26 @@ ROLE_POTENTIAL, ROLE_UX, ROLE_VY = 0, 1, 2
 
 
 class TileGeometry:
-    """Tiling used by the kernel: ``tx`` x ``ty`` cells per CTA (see stag_kernel.cuh)."""
+    """Tiling used by the kernel: ``tx`` x ``ty`` owned cells per tile, and how a
+    tile numbers its slots (layout 0: stag_kernel.cuh, layout 1: march_kernel.cuh)."""
 
-    def __init__(self, nx, ny, tx, ty, has_v):
+    def __init__(self, nx, ny, tx, ty, has_v, layout=0):
         self.nx, self.ny, self.tx, self.ty = int(nx), int(ny), int(tx), int(ty)
         self.has_v = bool(has_v)
+        self.layout = int(layout)
         self.tiles_x = (self.nx + self.tx - 1) // self.tx
         self.tiles_y = (self.ny + self.ty - 1) // self.ty
         self.ntiles = self.tiles_x * self.tiles_y
-        self.oy = 1 if has_v else 0
-        self.rx = self.tx + 3
+        if self.layout == 0:
+            # shared-memory region: one halo row above, columns x0-4 .. x0+tx+3
+            self.oy = 1 if has_v else 0
+            self.ox = 4
+            self.rx = self.tx + 8
+        else:
+            # register-marching warp strip: cells x0-1 .. x0+tx per row, rows from y0
+            self.oy = 0
+            self.ox = 1
+            self.rx = self.tx + 2
 
     def owner(self, cell):
         x = cell % self.nx
@@ -42,7 +52,7 @@ class TileGeometry:
         tx = x // self.tx
         ty = y // self.ty
         tile = ty * self.tiles_x + tx
-        pos = (y - ty * self.ty + self.oy) * self.rx + (x - tx * self.tx) + 1
+        pos = (y - ty * self.ty + self.oy) * self.rx + (x - tx * self.tx) + self.ox
         return tile, pos
 
     def placements(self, cell, role):
@@ -59,7 +69,7 @@ class TileGeometry:
                 tx = x[m] // self.tx - 1
                 ty = y[m] // self.ty
                 out_t.append(ty * self.tiles_x + tx)
-                out_p.append((y[m] - ty * self.ty + self.oy) * self.rx + self.tx + 1)
+                out_p.append((y[m] - ty * self.ty + self.oy) * self.rx + self.tx + self.ox)
                 out_s.append(src[m])
             # column 0 of row y is column nx of row y-1 (flat-index wrap)
             m = (x == 0) & (y > 0)
@@ -69,7 +79,7 @@ class TileGeometry:
                 ty = yy // self.ty
                 lx = self.nx - tx * self.tx
                 out_t.append(ty * self.tiles_x + tx)
-                out_p.append((yy - ty * self.ty + self.oy) * self.rx + lx + 1)
+                out_p.append((yy - ty * self.ty + self.oy) * self.rx + lx + self.ox)
                 out_s.append(src[m])
         elif role == ROLE_VY:
             m = (y % self.ty == 0) & (y > 0)
@@ -77,7 +87,7 @@ class TileGeometry:
                 tx = x[m] // self.tx
                 ty = y[m] // self.ty - 1
                 out_t.append(ty * self.tiles_x + tx)
-                out_p.append((self.ty + self.oy) * self.rx + (x[m] - tx * self.tx) + 1)
+                out_p.append((self.ty + self.oy) * self.rx + (x[m] - tx * self.tx) + self.ox)
                 out_s.append(src[m])
         return np.concatenate(out_t), np.concatenate(out_p), np.concatenate(out_s)
 
@@ -211,7 +221,7 @@ def compile_bounds(boundaries, n, pool, step_end, geo, role):
     ucells, start = np.unique(cells, return_index=True)
     end = np.append(start[1:], cells.size)
     tiles, pos, src = geo.placements(ucells, role)
-    o2 = np.argsort(tiles, kind="stable")
+    o2 = np.lexsort((pos, tiles))  # by tile, then slot (row-major within the tile)
     tiles, pos, src = tiles[o2], pos[o2], src[o2]
     groups = np.zeros(tiles.size, dtype=_capi.BOUND_GROUP_DTYPE)
     groups["cell"] = ucells[src]
@@ -235,7 +245,7 @@ def compile_probes(outputs, n, geo):
         return None, 0
     cols = np.arange(ncols)
     tiles, pos = geo.owner(cells)
-    o = np.argsort(tiles, kind="stable")
+    o = np.lexsort((cols, pos, tiles))
     probes = np.zeros(ncols, dtype=_capi.PROBE_DTYPE)
     probes["cell"] = cells[o]
     probes["pos"] = pos[o]

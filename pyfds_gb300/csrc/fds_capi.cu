@@ -58,16 +58,26 @@ int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, i
   return fds::tile_shape(flags, tile_x, tile_y);
 }
 
-int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t capacity) {
+int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, int32_t capacity) {
   int32_t k = 0;
-#define FDS_MENU_ENTRY(TX, TY, NT)               \
-  if (tile_x && tile_y && k < capacity) {        \
-    tile_x[k] = TX;                              \
-    tile_y[k] = TY;                              \
-  }                                              \
+#define FDS_MENU_ENTRY(TX, TY, NT)                    \
+  if (tile_x && tile_y && layout && k < capacity) {   \
+    tile_x[k] = TX;                                   \
+    tile_y[k] = TY;                                   \
+    layout[k] = 0;                                    \
+  }                                                   \
+  ++k;
+#define FDS_MARCH_ENTRY(CX, TY, NW)                   \
+  if (tile_x && tile_y && layout && k < capacity) {   \
+    tile_x[k] = 32 * CX - 2;                          \
+    tile_y[k] = TY;                                   \
+    layout[k] = 1;                                    \
+  }                                                   \
   ++k;
   FDS_TILE_MENU(FDS_MENU_ENTRY)
+  FDS_MARCH_MENU(FDS_MARCH_ENTRY)
 #undef FDS_MENU_ENTRY
+#undef FDS_MARCH_ENTRY
   return k;
 }
 

@@ -6,10 +6,14 @@
 
 #include "fds_capi.h"
 
-// Tile shapes (cells x, cells y, threads) built for the lossless 2-D variants: the
-// search space of the host-side autotuner. Every other variant uses the default
-// 64 x 16 (2-D) or 1024 x 1 (1-D) tile.
+// Tile shapes built for the lossless 2-D variants: the search space of the
+// host-side autotuner. Every other variant uses the default 64 x 16 (2-D) or
+// 1024 x 1 (1-D) shared-memory tile.
+//   FDS_TILE_MENU:  shared-memory tiles (cells x, cells y, threads); slot layout 0
+//   FDS_MARCH_MENU: register-marching warps (cells per lane CX, rows TY, warps per
+//                   CTA); the tile is (32*CX - 2) x TY cells; slot layout 1
 #define FDS_TILE_MENU(X) X(64, 16, 256) X(32, 32, 256) X(128, 8, 256) X(64, 32, 512) X(128, 16, 512)
+#define FDS_MARCH_MENU(X) X(2, 16, 4) X(2, 8, 4) X(2, 32, 4) X(1, 16, 4) X(1, 32, 4)
 
 namespace fds {
 

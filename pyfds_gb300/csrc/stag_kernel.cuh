@@ -4,7 +4,8 @@
 // 1-D / axisymmetric / thermal siblings). A CTA owns a TX x TY tile of cells and
 // stages in shared memory everything the step needs around it:
 //
-//   region  : columns x0-1 .. x0+TX+1, rows y0-1 .. y0+TY+1 (1-D: one row)
+//   region  : columns x0-4 .. x0+TX+3, rows y0-1 .. y0+TY+1 (1-D: one row); the
+//             4-column left margin keeps every row start 16-byte aligned for TMA
 //   sP      : potential (pressure / temperature) after this step's bounds
 //   sU, sV  : old flux, then the new flux over the "extended" regions
 //             U-ext = [x0, x1] x [y0, y1)   (one column right of the tile)
@@ -38,6 +39,7 @@
 #include <stdint.h>
 
 #include "fds_capi.h"
+#include "tma.cuh"
 
 namespace fds {
 
@@ -70,12 +72,18 @@ struct StagArgs {
   int32_t apply_next;
   int32_t store_flux;
   int32_t iso;  // by == bx and ky == kx: the y factors are not staged separately
+  int32_t ntiles;
+  int32_t use_tma;  // stage the region with TMA boxes (tm[]) instead of cp.async
+  int32_t* status;  // OR-ed with kStatus* bits; may be null
+  // tensor maps of the arrays staged per tile: P, U, V, Bx, Kx, By, Ky
+  CUtensorMap tm[7];
 };
 
 // Variant switches of the tile kernel.
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
-          bool EXACT_>
+          bool EXACT_, int STAGES_ = 1>
 struct StagCfg {
+  static constexpr int STAGES = STAGES_;  // staging buffers (2: persistent, prefetching)
   static constexpr int TX = TX_;
   static constexpr int TY = TY_;
   static constexpr int NT = NT_;
@@ -85,10 +93,11 @@ struct StagCfg {
   static constexpr bool AXI = AXI_;
   static constexpr bool EXACT = EXACT_;
   static constexpr int OY = HAS_V ? 1 : 0;  // region row of y0
-  static constexpr int RX = TX + 3;
+  static constexpr int OX = 4;               // region column of x0 (16-byte aligned start)
+  static constexpr int RX = TX + 8;          // region columns x0-4 .. x0+TX+3
   static constexpr int RY = HAS_V ? TY + 3 : TY;
   static constexpr int RN = RX * RY;
-  static constexpr int MIN_BLOCKS = HAS_V ? (NT >= 512 ? 2 : 4) : 2;
+  static constexpr int MIN_BLOCKS = STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : 4) : 2);
 };
 
 template <typename T>
@@ -208,111 +217,264 @@ __device__ __forceinline__ TF flux_new(const StagArgs<TP, TF, TC>& a, const TP* 
   }
 }
 
-// Dynamic shared memory of one CTA of this variant.
+// Shared memory of one staging buffer of this variant; every array starts on a
+// 128-byte boundary (TMA destinations).
+__host__ __device__ constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
+
 template <class C, typename TP, typename TF, typename TC>
-constexpr size_t stag_smem_bytes(bool iso) {
-  return (size_t)C::RN * (sizeof(TP) + (C::HAS_V ? 2 : 1) * sizeof(TF) +
-                          (iso || !C::HAS_V ? 2 : 4) * sizeof(TC));
+__host__ __device__ constexpr size_t stag_buffer_bytes(bool iso) {
+  return round128((size_t)C::RN * sizeof(TP)) +
+         (C::HAS_V ? 2 : 1) * round128((size_t)C::RN * sizeof(TF)) +
+         (iso || !C::HAS_V ? 2 : 4) * round128((size_t)C::RN * sizeof(TC));
 }
 
-template <class C, typename TP, typename TF, typename TC>
-__global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
-    stag_step_kernel(const StagArgs<TP, TF, TC> a) {
-  constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, RN = C::RN, OY = C::OY;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  TP* sP = reinterpret_cast<TP*>(smem_raw);
-  TF* sU = reinterpret_cast<TF*>(sP + RN);
-  TF* sV = sU + (C::HAS_V ? RN : 0);
-  TC* sBx = reinterpret_cast<TC*>(sV + RN);
-  TC* sKx = sBx + RN;
-  const bool iso = a.iso || !C::HAS_V;
-  TC* sBy = iso ? sBx : sKx + RN;
-  TC* sKy = iso ? sKx : sBy + RN;
+// The arrays of one staging buffer (see the region layout above).
+template <typename TP, typename TF, typename TC>
+struct StagBuf {
+  TP* P;
+  TF* U;
+  TF* V;
+  TC* Bx;
+  TC* Kx;
+  TC* By;
+  TC* Ky;
+};
 
-  const int tile = blockIdx.x;
-  const int tx = tile % a.tiles_x;
-  const int ty = tile / a.tiles_x;
-  const int x0 = tx * TX;
-  const int y0 = ty * TY;
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ StagBuf<TP, TF, TC> carve_buffer(unsigned char* base, bool iso) {
+  constexpr size_t RN = C::RN;
+  StagBuf<TP, TF, TC> b;
+  unsigned char* q = base;
+  b.P = reinterpret_cast<TP*>(q);
+  q += round128(RN * sizeof(TP));
+  b.U = reinterpret_cast<TF*>(q);
+  q += round128(RN * sizeof(TF));
+  b.V = C::HAS_V ? reinterpret_cast<TF*>(q) : b.U;
+  if (C::HAS_V) q += round128(RN * sizeof(TF));
+  b.Bx = reinterpret_cast<TC*>(q);
+  q += round128(RN * sizeof(TC));
+  b.Kx = reinterpret_cast<TC*>(q);
+  q += round128(RN * sizeof(TC));
+  if (iso || !C::HAS_V) {
+    b.By = b.Bx;
+    b.Ky = b.Kx;
+  } else {
+    b.By = reinterpret_cast<TC*>(q);
+    q += round128(RN * sizeof(TC));
+    b.Ky = reinterpret_cast<TC*>(q);
+  }
+  return b;
+}
+
+// Asynchronous global -> shared copy of one element (4 or 8 bytes); a slot whose
+// cell is out of range is zero-filled (source size 0, no bytes are read).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* base, int64_t f, bool ok) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
+  const T* src = base + (ok ? f : 0);
+  const int n = ok ? (int)sizeof(T) : 0;
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src), "r"(n)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(saddr), "l"(src), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Issue the copies of the potential, old flux and coefficients of one tile's region.
+// Slots are walked with incremental (column, row, flat index) updates.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void stage_tile(const StagArgs<TP, TF, TC>& a, int tile,
+                                           const StagBuf<TP, TF, TC>& b, bool iso) {
+  constexpr int NT = C::NT, RX = C::RX, RN = C::RN, OY = C::OY;
+  constexpr int DC = NT % RX, DR = NT / RX;
+  const int x0 = (tile % a.tiles_x) * C::TX;
+  const int y0 = (tile / a.tiles_x) * C::TY;
+  int c = threadIdx.x % RX;
+  int64_t f = (int64_t)(y0 + (int)threadIdx.x / RX - OY) * a.nx + (x0 + c - C::OX);
+  const int64_t df = (int64_t)DR * a.nx + DC;
+  const int64_t wrap = (int64_t)a.nx - RX;
+  for (int e = threadIdx.x; e < RN; e += NT) {
+    const bool ok = (f >= 0 && f < a.n);
+    cp_async_elem(b.P + e, a.p_in, f, ok);
+    if constexpr (C::MEMORY) {
+      cp_async_elem(b.U + e, a.u_in, f, ok);
+      if constexpr (C::HAS_V) cp_async_elem(b.V + e, a.v_in, f, ok);
+    }
+    cp_async_elem(b.Bx + e, a.bx, f, ok);
+    cp_async_elem(b.Kx + e, a.kx, f, ok);
+    if (!iso) {
+      cp_async_elem(b.By + e, a.by, f, ok);
+      cp_async_elem(b.Ky + e, a.ky, f, ok);
+    }
+    c += DC;
+    f += df;
+    if (c >= RX) {
+      c -= RX;
+      f += wrap;
+    }
+  }
+}
+
+// TMA staging of one tile's region: thread 0 issues one box per array into the
+// buffer, completing on `bar` (an mbarrier initialised for one arrival).
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void tma_issue_tile(const StagArgs<TP, TF, TC>& a, int tile,
+                                               const StagBuf<TP, TF, TC>& b, bool iso,
+                                               uint64_t* bar) {
+  constexpr int RN = C::RN;
+  const int gx = (tile % a.tiles_x) * C::TX - C::OX;
+  const int gy = (tile / a.tiles_x) * C::TY - C::OY;
+  uint32_t bytes = RN * (uint32_t)(sizeof(TP) + 2 * sizeof(TC));
+  if constexpr (C::MEMORY) bytes += (C::HAS_V ? 2 : 1) * RN * (uint32_t)sizeof(TF);
+  if (!iso) bytes += 2 * RN * (uint32_t)sizeof(TC);
+  // order the CTA's earlier generic accesses to this buffer (made visible to this
+  // thread by the preceding barrier) before the asynchronous-proxy writes
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  mbar_arrive_expect_tx(bar, bytes);
+  tma_load_2d(b.P, &a.tm[0], gx, gy, bar);
+  if constexpr (C::MEMORY) {
+    tma_load_2d(b.U, &a.tm[1], gx, gy, bar);
+    if constexpr (C::HAS_V) tma_load_2d(b.V, &a.tm[2], gx, gy, bar);
+  }
+  tma_load_2d(b.Bx, &a.tm[3], gx, gy, bar);
+  tma_load_2d(b.Kx, &a.tm[4], gx, gy, bar);
+  if (!iso) {
+    tma_load_2d(b.By, &a.tm[5], gx, gy, bar);
+    tma_load_2d(b.Ky, &a.tm[6], gx, gy, bar);
+  }
+}
+
+// Waits (bounded) for a tile's boxes, then patches the slots whose column lies
+// outside [0, nx): the box reads them as zeros, the flat-index semantics want the
+// cells of the neighbouring row. Returns false for every thread on a timeout.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ bool tma_finish_tile(const StagArgs<TP, TF, TC>& a, int tile,
+                                                const StagBuf<TP, TF, TC>& b, bool iso,
+                                                uint64_t* bar, uint32_t parity) {
+  constexpr int RX = C::RX, RN = C::RN, OX = C::OX, OY = C::OY, NT = C::NT;
+  constexpr long long kWaitLimit = 1ll << 22;
+  const int x0 = (tile % a.tiles_x) * C::TX;
+  const int y0 = (tile / a.tiles_x) * C::TY;
+  bool ok = mbar_wait(bar, parity, kWaitLimit);
+  if (__syncthreads_or(!ok)) {
+    // give the copies in flight a second bounded chance to land before leaving
+    if (!ok) mbar_wait(bar, parity, kWaitLimit);
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
+    return false;
+  }
+  if (x0 - OX < 0 || x0 - OX + RX > a.nx) {
+    for (int e = threadIdx.x; e < RN; e += NT) {
+      const int x = x0 - OX + e % RX;
+      if (x >= 0 && x < a.nx) continue;
+      const int64_t f = (int64_t)(y0 - OY + e / RX) * a.nx + x;
+      const bool in = (f >= 0 && f < a.n);
+      b.P[e] = in ? a.p_in[f] : TP(0);
+      if constexpr (C::MEMORY) {
+        b.U[e] = in ? a.u_in[f] : TF(0);
+        if constexpr (C::HAS_V) b.V[e] = in ? a.v_in[f] : TF(0);
+      }
+      b.Bx[e] = in ? a.bx[f] : TC(0);
+      b.Kx[e] = in ? a.kx[f] : TC(0);
+      if (!iso) {
+        b.By[e] = in ? a.by[f] : TC(0);
+        b.Ky[e] = in ? a.ky[f] : TC(0);
+      }
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// Everything after the region has landed: flux update, flux bounds and probes,
+// potential update, next step's potential bounds and probes, stores.
+//
+// Thread t owns the cells t + NT*k (k < OIT) of the TX x TY tile, TX a power of
+// two, and keeps their slot and flat index in registers through all phases. The
+// extended flux regions reach one column right (U) and one row down (V) of the
+// tile: inside a partial tile the owner of that slot computes it; past a full tile
+// the first TY threads compute the U column and the next TX threads the V row.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, int tile,
+                                             const StagBuf<TP, TF, TC>& b) {
+  constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, OY = C::OY;
+  constexpr int OIT = TX * TY / NT;
+  static_assert((TX & (TX - 1)) == 0, "tile width must be a power of two");
+  static_assert((TX * TY) % NT == 0, "the tile's cells must divide evenly among threads");
+  static_assert(!C::HAS_V || TX + TY <= NT, "halo threads: TX + TY must not exceed NT");
+  TP* sP = b.P;
+  TF* sU = b.U;
+  TF* sV = b.V;
+  const TC* sBx = b.Bx;
+  const TC* sKx = b.Kx;
+  const TC* sBy = b.By;
+  const TC* sKy = b.Ky;
+  const int x0 = (tile % a.tiles_x) * TX;
+  const int y0 = (tile / a.tiles_x) * TY;
   const int x1 = min(x0 + TX, a.nx);  // end of owned columns
   const int y1 = min(y0 + TY, a.ny);
   const int tid = threadIdx.x;
 
-  // ---- stage the potential, old flux and coefficients over the region ----
-  for (int e = tid; e < RN; e += NT) {
-    const int lx = e % RX - 1;
-    const int ly = e / RX - OY;
-    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
-    const bool ok = (f >= 0 && f < a.n);
-    sP[e] = ok ? a.p_in[f] : TP(0);
-    if constexpr (C::MEMORY) {
-      sU[e] = ok ? a.u_in[f] : TF(0);
-      if constexpr (C::HAS_V) sV[e] = ok ? a.v_in[f] : TF(0);
-    }
-    sBx[e] = ok ? __ldg(a.bx + f) : TC(0);
-    sKx[e] = ok ? __ldg(a.kx + f) : TC(0);
-    if (!iso) {
-      sBy[e] = ok ? __ldg(a.by + f) : TC(0);
-      sKy[e] = ok ? __ldg(a.ky + f) : TC(0);
-    }
+  int pos[OIT];
+  int64_t fo[OIT];
+  int xo[OIT];
+  bool own[OIT], inu[OIT], inv[OIT];
+#pragma unroll
+  for (int k = 0; k < OIT; ++k) {
+    const int c = tid + NT * k;
+    const int lx = c % TX;
+    const int ly = c / TX;
+    const int x = x0 + lx;
+    const int y = y0 + ly;
+    pos[k] = (ly + OY) * RX + lx + C::OX;
+    fo[k] = (int64_t)y * a.nx + x;
+    xo[k] = x;
+    own[k] = (x < x1 && y < y1);
+    inu[k] = (x <= x1 && y < y1 && fo[k] < a.n);  // U-ext, incl. a partial tile's edge
+    inv[k] = (x < x1 && y <= y1 && fo[k] < a.n);  // V-ext, incl. a partial tile's edge
   }
-  __syncthreads();
+  // halo threads past a full tile
+  const bool hu = (tid < TY) && (x1 == x0 + TX);
+  const bool hv = C::HAS_V && (tid >= TY) && (tid < TY + TX) && (y1 == y0 + TY);
+  const int hu_pos = (tid + OY) * RX + TX + C::OX;
+  const int64_t hu_f = (int64_t)(y0 + tid) * a.nx + x1;
+  const int hv_lx = tid - TY;
+  const int hv_pos = (TY + OY) * RX + hv_lx + C::OX;
+  const int64_t hv_f = (int64_t)y1 * a.nx + x0 + hv_lx;
 
-  // ---- flux update over U-ext and V-ext, kept in registers ----
-  constexpr int UC = (TX + 1) * TY;
-  constexpr int UIT = (UC + NT - 1) / NT;
-  constexpr int VC = C::HAS_V ? TX * (TY + 1) : 0;
-  constexpr int VIT = C::HAS_V ? (VC + NT - 1) / NT : 0;
-  TF un[UIT];
-  TF vn[VIT > 0 ? VIT : 1];
+  // ---- new fluxes over U-ext and V-ext ----
+  TF un[OIT], vn[OIT];
 #pragma unroll
-  for (int k = 0; k < UIT; ++k) {
-    const int e = tid + k * NT;
-    un[k] = TF(0);
-    if (e < UC) {
-      const int lx = e % (TX + 1);
-      const int ly = e / (TX + 1);
-      const int x = x0 + lx;
-      const int y = y0 + ly;
-      const int64_t f = (int64_t)y * a.nx + x;
-      if (x <= x1 && y < y1 && f < a.n) {
-        const int pos = (ly + OY) * RX + lx + 1;
-        const int xr = (x == a.nx) ? 0 : x;  // column of the wrapped halo cell
-        un[k] = flux_new<C, true>(a, sP, sU, sBx, pos, f, xr);
-      }
-    }
+  for (int k = 0; k < OIT; ++k) {
+    un[k] = inu[k] ? flux_new<C, true>(a, sP, sU, sBx, pos[k], fo[k],
+                                       xo[k] == a.nx ? 0 : xo[k])
+                   : TF(0);
+    if constexpr (C::HAS_V)
+      vn[k] = inv[k] ? flux_new<C, false>(a, sP, sV, sBy, pos[k], fo[k], xo[k]) : TF(0);
   }
-  if constexpr (C::HAS_V) {
+  TF uh = TF(0), vh = TF(0);
+  const bool hu_ok = hu && (y0 + tid < y1) && hu_f < a.n;
+  if (hu_ok) uh = flux_new<C, true>(a, sP, sU, sBx, hu_pos, hu_f, x1 == a.nx ? 0 : x1);
+  const bool hv_ok = hv && (x0 + hv_lx < x1) && hv_f < a.n;
+  if constexpr (C::HAS_V)
+    if (hv_ok) vh = flux_new<C, false>(a, sP, sV, sBy, hv_pos, hv_f, x0 + hv_lx);
+  if constexpr (C::MEMORY && C::ABSORB) __syncthreads();  // neighbours read the old flux
 #pragma unroll
-    for (int k = 0; k < VIT; ++k) {
-      const int e = tid + k * NT;
-      vn[k] = TF(0);
-      if (e < VC) {
-        const int lx = e % TX;
-        const int ly = e / TX;
-        const int x = x0 + lx;
-        const int y = y0 + ly;
-        const int64_t f = (int64_t)y * a.nx + x;
-        if (x < x1 && y <= y1 && f < a.n) {
-          const int pos = (ly + OY) * RX + lx + 1;
-          vn[k] = flux_new<C, false>(a, sP, sV, sBy, pos, f, x);
-        }
-      }
-    }
+  for (int k = 0; k < OIT; ++k) {
+    sU[pos[k]] = un[k];
+    if constexpr (C::HAS_V) sV[pos[k]] = vn[k];
   }
-  if constexpr (C::MEMORY && C::ABSORB) __syncthreads();  // neighbours read old flux
-#pragma unroll
-  for (int k = 0; k < UIT; ++k) {
-    const int e = tid + k * NT;
-    if (e < UC) sU[(e / (TX + 1) + OY) * RX + e % (TX + 1) + 1] = un[k];
-  }
-  if constexpr (C::HAS_V) {
-#pragma unroll
-    for (int k = 0; k < VIT; ++k) {
-      const int e = tid + k * NT;
-      if (e < VC) sV[(e / TX + OY) * RX + e % TX + 1] = vn[k];
-    }
-  }
+  if (hu) sU[hu_pos] = uh;
+  if constexpr (C::HAS_V)
+    if (hv) sV[hv_pos] = vh;
   __syncthreads();
 
   // ---- flux bounds and probes (this step) ----
@@ -323,39 +485,32 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
   if constexpr (C::HAS_V) write_probes<NT>(a.tab[2], tile, sV, a.step - a.step0);
 
   // ---- potential update of the owned cells ----
-  constexpr int OC = TX * TY;
-  constexpr int OIT = (OC + NT - 1) / NT;
   TP pn[OIT];
 #pragma unroll
   for (int k = 0; k < OIT; ++k) {
-    const int e = tid + k * NT;
-    const int lx = e % TX;
-    const int ly = e / TX;
-    const int x = x0 + lx;
-    const int y = y0 + ly;
-    const int64_t f = (int64_t)y * a.nx + x;
+    const int ps = pos[k];
     pn[k] = TP(0);
-    if (e < OC && x < x1 && y < y1) {
-      const int pos = (ly + OY) * RX + lx + 1;
-      if (a.store_flux) {
-        a.u_out[f] = sU[pos];
-        if constexpr (C::HAS_V) a.v_out[f] = sV[pos];
-      }
-      const TF kxi = (TF)sKx[pos];
-      const TF kxn = (TF)sKx[pos + 1];
-      const TF u = sU[pos];
-      const TF un1 = sU[pos + 1];
-      TF kyi = TF(0), kyn = TF(0), v = TF(0), vn1 = TF(0);
+    if (own[k]) {
+      const TF u = sU[ps];
+      const TF un1 = sU[ps + 1];
+      TF v = TF(0), vn1 = TF(0), kyi = TF(0), kyn = TF(0);
       if constexpr (C::HAS_V) {
-        kyi = (TF)sKy[pos];
-        kyn = (TF)sKy[pos + RX];
-        v = sV[pos];
-        vn1 = sV[pos + RX];
+        v = sV[ps];
+        vn1 = sV[ps + RX];
+        kyi = (TF)sKy[ps];
+        kyn = (TF)sKy[ps + RX];
       }
+      if (a.store_flux) {
+        a.u_out[fo[k]] = u;
+        if constexpr (C::HAS_V) a.v_out[fo[k]] = v;
+      }
+      const TF kxi = (TF)sKx[ps];
+      const TF kxn = (TF)sKx[ps + 1];
       if constexpr (C::EXACT) {
         TF w = u, wn = un1;
         if constexpr (C::AXI) {
           // a_p_vx.dot(vx * r): the flux is scaled by the radius of its column
+          const int x = xo[k];
           const int xn = (x + 1 == a.nx) ? 0 : x + 1;
           w = xmul(u, (TF)__ldg(a.rx + x));
           wn = xmul(un1, (TF)__ldg(a.rx + xn));
@@ -366,9 +521,9 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
           const TF sy = xadd(-xmul(kyi, v), xmul(kyn, vn1));
           sx = xadd(sx, sy);
         }
-        pn[k] = (TP)xsub((TF)sP[pos], sx);
+        pn[k] = (TP)xsub((TF)sP[ps], sx);
       } else if constexpr (sizeof(TP) == sizeof(TF)) {
-        TF acc = (TF)sP[pos];
+        TF acc = (TF)sP[ps];
         acc = fma(kxi, u, acc);
         acc = fma(-kxn, un1, acc);
         if constexpr (C::HAS_V) {
@@ -384,32 +539,89 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
           inc = fma(kyi, v, inc);
           inc = fma(-kyn, vn1, inc);
         }
-        pn[k] = sP[pos] + (TP)inc;
+        pn[k] = sP[ps] + (TP)inc;
       }
     }
   }
   __syncthreads();  // all reads of sP done
 #pragma unroll
-  for (int k = 0; k < OIT; ++k) {
-    const int e = tid + k * NT;
-    if (e < OC) sP[(e / TX + OY) * RX + e % TX + 1] = pn[k];
-  }
+  for (int k = 0; k < OIT; ++k)
+    if (own[k]) sP[pos[k]] = pn[k];
   if (a.apply_next) {
     __syncthreads();
     apply_bound_groups<NT>(a.tab[0], tile, sP, a.pool, a.step + 1);
     __syncthreads();
     write_probes<NT>(a.tab[0], tile, sP, a.step + 1 - a.step0);
+#pragma unroll
+    for (int k = 0; k < OIT; ++k)
+      if (own[k]) pn[k] = sP[pos[k]];
   }
   // ---- store the owned potential ----
 #pragma unroll
-  for (int k = 0; k < OIT; ++k) {
-    const int e = tid + k * NT;
-    const int lx = e % TX;
-    const int ly = e / TX;
-    const int x = x0 + lx;
-    const int y = y0 + ly;
-    if (e < OC && x < x1 && y < y1) {
-      a.p_out[(int64_t)y * a.nx + x] = sP[(ly + OY) * RX + lx + 1];
+  for (int k = 0; k < OIT; ++k)
+    if (own[k]) a.p_out[fo[k]] = pn[k];
+}
+
+// Grid-stride over tiles. STAGES == 1: one tile per CTA, staged then computed.
+// STAGES == 2 (persistent CTAs): the copies of the next tile are in flight while
+// the current tile is computed from the other buffer. Staging is TMA when the
+// launch provides tensor maps (use_tma) and cp.async otherwise.
+template <class C, typename TP, typename TF, typename TC>
+__global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
+    stag_step_kernel(const __grid_constant__ StagArgs<TP, TF, TC> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const bool iso = a.iso || !C::HAS_V;
+  const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(iso);
+  // the TMA barriers follow the buffers; TMA needs 128-byte aligned destinations
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + C::STAGES * bytes);
+  const bool tma = a.use_tma && (smem_addr(smem_raw) & 127u) == 0;
+  const StagBuf<TP, TF, TC> buf0 = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
+  int t = blockIdx.x;
+  if (tma && threadIdx.x == 0)
+    for (int k = 0; k < C::STAGES; ++k) mbar_init(bars + k, 1);
+  __syncthreads();
+  if constexpr (C::STAGES == 1) {
+    if (tma) {
+      if (threadIdx.x == 0) tma_issue_tile<C>(a, t, buf0, iso, bars);
+      if (!tma_finish_tile<C>(a, t, buf0, iso, bars, 0)) return;
+    } else {
+      stage_tile<C>(a, t, buf0, iso);
+      cp_async_commit();
+      cp_async_wait<0>();
+      __syncthreads();
+    }
+    compute_tile<C>(a, t, buf0);
+  } else {
+    const StagBuf<TP, TF, TC> buf1 = carve_buffer<C, TP, TF, TC>(smem_raw + bytes, iso);
+    const int stride = gridDim.x;
+    if (t < a.ntiles) {
+      if (tma) {
+        if (threadIdx.x == 0) tma_issue_tile<C>(a, t, buf0, iso, bars);
+      } else {
+        stage_tile<C>(a, t, buf0, iso);
+      }
+    }
+    if (!tma) cp_async_commit();
+    for (int k = 0; t < a.ntiles; ++k, t += stride) {
+      const int tn = t + stride;
+      const int cur = k & 1;
+      __syncthreads();  // every thread is done with the buffer the next copies fill
+      if (tn < a.ntiles) {
+        if (tma) {
+          if (threadIdx.x == 0) tma_issue_tile<C>(a, tn, cur ? buf0 : buf1, iso, bars + (cur ^ 1));
+        } else {
+          stage_tile<C>(a, tn, cur ? buf0 : buf1, iso);
+        }
+      }
+      if (tma) {
+        // buffer `cur` completes once per use: its (k >> 1)-th use has parity (k >> 1) & 1
+        if (!tma_finish_tile<C>(a, t, cur ? buf1 : buf0, iso, bars + cur, (k >> 1) & 1)) return;
+      } else {
+        cp_async_commit();
+        cp_async_wait<1>();  // this thread's copies of tile t have landed
+        __syncthreads();     // ... and every other thread's
+      }
+      compute_tile<C>(a, t, cur ? buf1 : buf0);
     }
   }
 }

@@ -146,7 +146,7 @@ class KernelModel:
                 x1, y1 = min(x0 + geo.tx, nx), min(y0 + geo.ty, geo.ny)
                 flat = np.zeros(RX * RY, dtype=np.int64)
                 for e in range(RX * RY):
-                    flat[e] = (y0 + e // RX - OY) * nx + x0 + e % RX - 1
+                    flat[e] = (y0 + e // RX - OY) * nx + x0 + e % RX - geo.ox
                 ok = (flat >= 0) & (flat < n)
                 sP = np.where(ok, st[0][np.clip(flat, 0, n - 1)], 0.0)
                 sU = np.where(ok, st[1][np.clip(flat, 0, n - 1)], 0.0) if self.memory \
@@ -183,7 +183,7 @@ class KernelModel:
                     for lx in range(geo.tx + 1):
                         x, y = x0 + lx, y0 + ly
                         i = y * nx + x
-                        pos = (ly + OY) * RX + lx + 1
+                        pos = (ly + OY) * RX + lx + geo.ox
                         val = 0.0
                         if x <= x1 and y < y1 and i < n:
                             val = fluxnew(True, pos, i, 0 if x == nx else x, sU)
@@ -194,7 +194,7 @@ class KernelModel:
                         for lx in range(geo.tx):
                             x, y = x0 + lx, y0 + ly
                             i = y * nx + x
-                            pos = (ly + OY) * RX + lx + 1
+                            pos = (ly + OY) * RX + lx + geo.ox
                             val = 0.0
                             if x < x1 and y <= y1 and i < n:
                                 val = fluxnew(False, pos, i, x, sV)
@@ -216,7 +216,7 @@ class KernelModel:
                         if x >= x1 or y >= y1:
                             continue
                         i = y * nx + x
-                        pos = (ly + OY) * RX + lx + 1
+                        pos = (ly + OY) * RX + lx + geo.ox
                         new[1][i] = sU[pos]
                         if self.has_v:
                             new[2][i] = sV[pos]
@@ -238,7 +238,7 @@ class KernelModel:
                     for lx in range(geo.tx):
                         x, y = x0 + lx, y0 + ly
                         if x < x1 and y < y1:
-                            new[0][y * nx + x] = sP[(ly + OY) * RX + lx + 1]
+                            new[0][y * nx + x] = sP[(ly + OY) * RX + lx + geo.ox]
             st = new
         state = {name: st[k] for k, name in enumerate(comps)}
         sig = {}

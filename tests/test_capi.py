@@ -45,7 +45,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_capi.FdsStagProblem) == 8 * 4 + 11 * 8
     assert C.sizeof(_capi.FdsStagState) == 6 * 8
     assert C.sizeof(_capi.FdsCompTables) == 6 * 8 + 8
-    assert C.sizeof(_capi.FdsStagTables) == 3 * 56 + 16
+    assert C.sizeof(_capi.FdsStagTables) == 3 * 56 + 24
     assert _capi.BOUND_OP_DTYPE.itemsize == 32
     assert _capi.BOUND_GROUP_DTYPE.itemsize == 24
     assert _capi.PROBE_DTYPE.itemsize == 16

@@ -239,18 +239,33 @@ def test_thermal_f32_t64_error_vs_float64(gpu):
     assert err <= 1e-2, err
 
 
-@pytest.mark.parametrize("tile", [(64, 16), (32, 32), (128, 8), (64, 32), (128, 16)])
+MENU = [((64, 16), 1), ((32, 32), 1), ((128, 8), 1), ((64, 32), 1), ((128, 16), 1),
+        ((64, 16), 2), ((32, 32), 2), ((128, 8), 2), ((64, 32), 2), ((128, 16), 2),
+        ((62, 16), 1), ((62, 8), 1), ((62, 32), 1), ((30, 16), 1), ((30, 32), 1)]
+
+
+@pytest.mark.parametrize("nx", [203, 204])  # 204: rows are 16-byte multiples -> TMA staging
+@pytest.mark.parametrize("tile,stages", MENU)
 @pytest.mark.parametrize("kind", ["Acoustic2D", "Thermal2D"])
-def test_tile_menu_parity(gpu, tile, kind):
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_tile_menu_parity(gpu, tile, kind, stages, precision, nx):
     """Every tile shape of the autotuner's menu against the oracle (grids that are not
     multiples of the tile, so partial tiles and row-end wraps cross tile seams)."""
     from pyfds_gb300 import _capi
     assert tile in _capi.tile_menu()
-    spec = S.random_scenario(21, kind, 203, 77, steps=15, mu=False)
+    spec = S.random_scenario(21, kind, nx, 77, steps=15, mu=False)
     st_o, sg_o = O.simulate(spec, spec["steps"])
-    f = build_field(spec, tile=tile)
-    f.simulate(spec["steps"])
+    from pyfds_gb300 import _capi as capi
+    f = build_field(spec, tile=tile, precision=precision)
+    f.stages = stages
+    try:
+        f.simulate(spec["steps"])
+    except capi.FdsError as e:
+        if e.code == capi.FDS_E_SIZE:
+            pytest.skip("does not fit in shared memory: %s" % e)
+        raise
     st, sig = field_results(f)
-    assert max_rel_l2_signals(sig, sg_o) <= TOL
+    tol = TOL if precision == "f64" else 1e-5
+    assert max_rel_l2_signals(sig, sg_o) <= tol
     for c in st_o:
-        assert rel_l2(st[c], st_o[c]) <= TOL, c
+        assert rel_l2(st[c], st_o[c]) <= tol, c

@@ -85,3 +85,58 @@ def test_negative_indices_wrap_like_numpy():
     f = build_field(spec, exact=True)
     st_m, _ = KernelModel(f, tile=(4, 1)).run(spec["steps"])
     assert np.array_equal(st_o["pressure"], st_m["pressure"])
+
+
+def _decode(geo, tile, pos):
+    """Flat cell of a tile slot (inverse of the slot numbering of each layout)."""
+    tx, ty = tile % geo.tiles_x, tile // geo.tiles_x
+    x0, y0 = tx * geo.tx, ty * geo.ty
+    lx = pos % geo.rx - geo.ox
+    ly = pos // geo.rx - geo.oy
+    return (y0 + ly) * geo.nx + x0 + lx
+
+
+@pytest.mark.parametrize("layout,tile", [(0, (64, 16)), (0, (4, 3)), (1, (62, 16)), (1, (30, 8)),
+                                         (1, (6, 3))])
+@pytest.mark.parametrize("nx,ny", [(200, 77), (62, 31), (7, 40), (130, 9)])
+def test_table_slots_decode_to_their_cells(layout, tile, nx, ny):
+    """Every boundary group and probe sits in slots that hold its own cell, and each
+    flux cell is present in every tile that reads it (owner, right/bottom halo,
+    row-end wrap)."""
+    from pyfds_gb300 import _tables
+    import pyfds_gb300 as fds
+    from pyfds_gb300.regions import Region
+    geo = _tables.TileGeometry(nx, ny, tile[0], tile[1], True, layout)
+    n = nx * ny
+    rng = np.random.default_rng(nx * 1000 + ny)
+    cells = np.unique(np.concatenate([rng.integers(0, n, 300), np.arange(0, n, nx),
+                                      np.arange(nx - 1, n, nx), np.arange(nx)]))
+    for role in (0, 1, 2):
+        b = fds.Boundary(Region(cells), value=1.0)
+        bt = _tables.compile_bounds([b], n, _tables.SignalPool(), 1, geo, role)
+        ts = bt["tile_start"]
+        for t in range(geo.ntiles):
+            grp = bt["groups"][ts[t]:ts[t + 1]]
+            assert np.all(np.diff(grp["pos"]) >= 0)  # sorted by slot within a tile
+            for g in grp:
+                assert _decode(geo, t, g["pos"]) == g["cell"]
+        # each flux cell appears in the tiles whose extended region reads it
+        placed = {(int(t), int(g["cell"])) for t in range(geo.ntiles)
+                  for g in bt["groups"][ts[t]:ts[t + 1]]}
+        for t in range(geo.ntiles):
+            x0, y0 = (t % geo.tiles_x) * geo.tx, (t // geo.tiles_x) * geo.ty
+            x1, y1 = min(x0 + geo.tx, nx), min(y0 + geo.ty, ny)
+            if role == 1:   # U-ext: [x0, x1] x [y0, y1)
+                need = [(y * nx + x) for y in range(y0, y1) for x in range(x0, x1 + 1)]
+            elif role == 2:  # V-ext: [x0, x1) x [y0, y1]
+                need = [(y * nx + x) for y in range(y0, y1 + 1) for x in range(x0, x1)]
+            else:
+                need = [(y * nx + x) for y in range(y0, y1) for x in range(x0, x1)]
+            for c in need:
+                if c < n and c in set(cells.tolist()):
+                    assert (t, c) in placed, (role, t, c)
+    pt, ncols = _tables.compile_probes([fds.Output(Region(cells))], n, geo)
+    ts = pt["tile_start"]
+    for t in range(geo.ntiles):
+        for q in pt["probes"][ts[t]:ts[t + 1]]:
+            assert _decode(geo, t, q["pos"]) == q["cell"]
