@@ -36,9 +36,11 @@ WORKLOADS = {
     "acoustic1d": ("acoustic1d_water", {}, {"f64": 48, "f32": 24}),
     "axi": ("axi_disc_source", {}, {"f64": 64, "f32": 32}),
     "thermal": ("thermal2d_two_materials", {"nt": 2000}, {"f64": 32, "f32": 16, "f32_t64": 24}),
+    "batched": ("layered_media_batch", {}, {"f64": 64, "f32": 32}),
 }
 # CPU sample per process and step of the reference arm (time steps), per workload
-CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 10}
+CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 10,
+                    "batched": 60}
 L2_BYTES = 129 * 2 ** 20
 
 
@@ -125,6 +127,19 @@ def cpu_sample(wname, steps_per_proc, procs, repeats=1, warmup=0):
     from oracle import bench_worker
     builder, kwargs, _ = WORKLOADS[wname]
     ctx = mp.get_context("spawn")
+    if wname == "batched":
+        # one batch instance per process, run concurrently
+        with ctx.Pool(procs) as pool:
+            vals = []
+            tasks = [(builder, kwargs, k, steps_per_proc) for k in range(procs)]
+            pool.map(bench_worker.run_batch_instance,
+                     [(builder, kwargs, k, 1) for k in range(procs)], chunksize=1)
+            for r in range(warmup + repeats):
+                res = pool.map(bench_worker.run_batch_instance, tasks, chunksize=1)
+                if r >= warmup:
+                    vals.append(sum(c * steps_per_proc for c, _ in res) / max(t for _, t in res)
+                                / 1e9)
+            return vals, sum(c for c, _ in res)
     with ctx.Pool(procs, initializer=bench_worker.setup, initargs=(builder, kwargs)) as pool:
         cells = pool.apply(bench_worker.cells)
         pool.map(bench_worker.run, [1] * procs)  # touch every replica once
@@ -159,6 +174,136 @@ def run_reference(args):
                                        % (steps, procs)},
             "e2e": {"value": v, "unit": "Gcell/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batched(args):
+    """The layered-media batch: one launch per step for all instances, the whole
+    run replayed from a CUDA graph; e2e through simulate_batch with host buffers."""
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pyfds_gb300 import workloads
+    from pyfds_gb300.batch import BatchRunner, simulate_batch
+    builder, kwargs, balg = WORKLOADS["batched"]
+    kwargs = dict(kwargs)
+    if args.time_steps:
+        kwargs["nt"] = args.time_steps
+    if args.batch:
+        kwargs["count"] = args.batch
+    specs = getattr(workloads, builder)(**kwargs)
+    nt = int(specs[0]["steps"])
+    fields = [workloads.build_field(sp, precision=args.precision) for sp in specs]
+    cells = sum(f.num_points for f in fields)
+    tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else (64, 16)
+    stages = args.stages or 1
+    if args.autotune:
+        from pyfds_gb300.autotune import autotune_batch
+        tile, stages = autotune_batch(fields, steps=20)
+    runner = BatchRunner(fields, nt, tile=tile, stages=stages)
+    runner.capture()
+
+    def reset():
+        for f in fields:
+            for bufs in f._engine().buffers.values():
+                for t in bufs:
+                    t.zero_()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        reset()
+        runner.replay()
+    barrier()
+    stream = torch.cuda.current_stream()
+    total_ms = 0.0
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            reset()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            runner.replay()
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+    barrier()
+    ms = total_ms / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * cells * nt / (ms * 1e-3) / 1e9
+    launch_ms = ms / nt
+    # e2e: the public API with host state and host outputs, every step
+    e2e_steps = 0 if args.no_e2e else 1
+    h2d = d2h = 0
+    e2e_value = None
+    if e2e_steps:
+        barrier()
+        t0 = time.perf_counter()
+        for f in fields:
+            for name in f._stag_components:
+                getattr(f, name).values = np.zeros(f.num_points)
+            f._coef_version += 1
+            f.step = 0
+            for o in f.pressure.outputs:
+                o.signals = []
+        r = simulate_batch(fields, nt, tile=tile, stages=stages)
+        finals = [f.pressure.values for f in fields]
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        e2e_value = ws * cells * nt / e2e_s / 1e9
+        esz = 8 if args.precision == "f64" else 4
+        h2d = sum(f.num_points * esz * 5 for f in fields) + sum(
+            int(p["tabs"]["blob"].numel()) for p in r.plans) + int(r.workspace.numel())
+        d2h = sum(sum(o.numel() * 8 for o in p["outs"] if o is not None) for p in r.plans) + \
+            sum(a.size * esz for a in finals)
+    if rank != 0:
+        return 0
+    peak, peak_kind = _peaks()
+    bpc = balg.get(args.precision)
+    achieved = cells * bpc / (launch_ms * 1e-3) / 1e9 if bpc else None
+    line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.precision, "data": "synthetic (seeded layered media, no dataset)",
+            "config": {"workload": "batched: %d layered-media Acoustic2D instances, n in "
+                                   "[128, 1024] log-uniform, %d steps each" % (len(fields), nt),
+                       "cells": cells, "time_steps_per_step": nt, "precision": args.precision,
+                       "tile": "%dx%d" % tuple(tile), "stages": stages,
+                       "launch": "one kernel per time step for all instances, whole run "
+                                 "replayed from one CUDA graph",
+                       "l2": "inputs larger than L2 (%.0f MB of state)"
+                             % (cells * 6 * (8 if args.precision == "f64" else 4) / 2 ** 20),
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": _traffic_from_profiles("batched_%s" % args.precision),
+                         "peak_kind": peak_kind, "kernel": "stag_batch_kernel",
+                         "bytes_per_cell": bpc, "launch_ms": launch_ms},
+            "clocks": clk.summary(),
+            "gpu_launches": int(args.steps * (nt + 1))}
+    if ws == 1 and not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        steps = CPU_SAMPLE_STEPS["batched"]
+        vals, _ = cpu_sample("batched", steps, procs, repeats=1)
+        line["cpu_baseline"] = {"value": vals[0], "unit": "Gcell/s", "cores": procs,
+                                "kind": "port",
+                                "sample": "%d time steps of one batch instance per process, "
+                                          "%d processes (the first %d instances), numpy oracle"
+                                          % (steps, procs, procs)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -318,11 +463,15 @@ def main():
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
     ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2],
                     help="staging buffers per CTA (0: automatic)")
+    ap.add_argument("--batch", type=int, default=0, help="instances of the batched workload")
+    ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")
     ap.add_argument("--time-steps", type=int, default=0,
                     help="override the workload's time steps per benchmark step (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

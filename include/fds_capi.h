@@ -105,8 +105,8 @@ typedef struct FdsStagProblem {
   int32_t tile_x; /* tile shape the tables below were built for: the default of */
   int32_t tile_y; /* fds_stag_tile_shape, or for lossless 2-D non-exact variants any
                      shape listed by fds_stag_tile_menu */
-  int32_t stages; /* 0: automatic; 1: one CTA per tile; 2: persistent CTAs that prefetch
-                     the next tile while computing one (lossless 2-D variants) */
+  int32_t stages; /* 0 (automatic) or 1: one CTA per tile; 2: persistent CTAs that
+                     prefetch the next tile while computing one (lossless 2-D variants) */
   FdsCoefs coefs;
 } FdsStagProblem;
 
@@ -212,6 +212,34 @@ int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, in
 int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps,
                      int32_t store_flux, void* stream);
+
+/* Workspace (device bytes, 256-byte aligned) a batched call over `count` instances
+ * with `total_tiles` tiles in all needs: per-instance descriptors and the work
+ * list. (New: no reference counterpart; the reference runs one field at a time.) */
+size_t fds_stag_batch_workspace_bytes(int32_t count, int64_t total_tiles);
+
+/*
+ * Advance `count` independent fields by `nsteps` steps each with one kernel
+ * launch per step covering every tile of every instance (plus one prologue
+ * launch). Each instance i is `probs[i]` / `states[i]` / `tables[i]` exactly as
+ * for fds_stag_run; all instances share family, precision, flags, tile and stages
+ * (lossless 2-D, non-exact variants), and may differ in grid size and media.
+ * Equivalent to calling fds_stag_run on each instance (the reference's
+ * `Field.simulate`, pyfds/fields.py:67-95, once per field); the descriptors and
+ * work list are written into the caller's `workspace` (see
+ * fds_stag_batch_workspace_bytes) by an asynchronous copy on `stream`.
+ * `mode`: FDS_BATCH_UPLOAD writes the descriptors (host work + a copy);
+ * FDS_BATCH_LAUNCH enqueues the kernels only (no host-side copies, so it can be
+ * captured into a CUDA graph) and needs a workspace uploaded with the same
+ * arguments; both bits do both. After the launch phase the state pointers of
+ * every instance are swapped as many times as steps ran.
+ */
+#define FDS_BATCH_UPLOAD 1u
+#define FDS_BATCH_LAUNCH 2u
+int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
+                           const FdsStagTables* tables, int32_t count, void* workspace,
+                           size_t workspace_bytes, int64_t step0, int32_t nsteps,
+                           int32_t store_flux, uint32_t mode, void* stream);
 
 #ifdef __cplusplus
 }

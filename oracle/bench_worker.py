@@ -43,3 +43,25 @@ def run(nsteps):
 
 def cells():
     return int(_W["ops"]["n"])
+
+
+_BATCH = {}
+
+
+def run_batch_instance(args):
+    """(cells, seconds) of ``nsteps`` oracle steps on instance k of a batch workload."""
+    workload, kwargs, k, nsteps = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from pyfds_gb300 import workloads
+    if k not in _BATCH:
+        spec = getattr(workloads, workload)(**kwargs)[k]
+        ops = O.assemble(spec)
+        _BATCH[k] = (spec, ops, {c: np.zeros(ops["n"]) for c in O.components_of(spec["kind"])})
+    spec, ops, state = _BATCH[k]
+    outputs = spec.get("outputs") or {}
+    signals = {c: [[[] for _ in idx] for idx in outputs.get(c, [])] for c in state}
+    t0 = time.perf_counter()
+    for s in range(nsteps):
+        O.sim_step(spec["kind"], ops, state, spec.get("bounds") or {}, outputs, signals, s,
+                   dt=spec["dt"])
+    return int(ops["n"]), time.perf_counter() - t0

@@ -1,0 +1,124 @@
+"""Batched time stepping: many independent 2-D fields advanced together.
+
+``simulate_batch(fields, n)`` is equivalent to ``f.simulate(n)`` for every field
+(pyfds/fields.py:67-95 once per field), but each time step is ONE kernel launch
+covering every tile of every field (``fds_stag_batch_run``). The fields may differ
+in grid size, media, boundaries and outputs; they must share the class, the
+precision and the tile shape, be lossless 2-D fields (no absorption, not
+``exact``) and stand at the same step.
+
+``BatchRunner`` splits the call into an upload phase (descriptors, tables) and a
+launch-only phase, so the launch sequence of a run can be captured once in a CUDA
+graph and replayed (parameter sweeps that reset and rerun the same set of fields).
+"""
+import ctypes as C
+
+from . import _capi
+from ._engine import require_cuda
+
+
+class BatchRunner:
+    """Device-side plan of one batched run of ``num_steps`` steps."""
+
+    def __init__(self, fields, num_steps, tile=None, stages=None):
+        if not fields:
+            raise ValueError("empty batch")
+        self.torch = require_cuda()
+        self.fields = list(fields)
+        self.num_steps = int(num_steps)
+        f0 = self.fields[0]
+        for f in self.fields:
+            if type(f) is not type(f0) or f.precision != f0.precision:
+                raise ValueError("batched fields must share class and precision")
+            if f.step != f0.step:
+                raise ValueError("batched fields must stand at the same step")
+            if tile is not None:
+                f.tile = tuple(tile)
+            if stages is not None:
+                f.stages = int(stages)
+            if not f.matrices_assembled:
+                f.assemble_matrices()
+        self.step0 = int(f0.step)
+        self.plans = [f._engine().prepare(self.step0, self.num_steps) for f in self.fields]
+        n = len(self.fields)
+        self.probs = (_capi.FdsStagProblem * n)(*[p["prob"] for p in self.plans])
+        self.tables = (_capi.FdsStagTables * n)(*[p["tstruct"] for p in self.plans])
+        self.states = (_capi.FdsStagState * n)()
+        self.total_tiles = sum(p["geo"].ntiles for p in self.plans)
+        lib = _capi.load()
+        nbytes = lib.fds_stag_batch_workspace_bytes(n, self.total_tiles)
+        dev = self.torch.device("cuda", self.torch.cuda.current_device())
+        self.workspace = self.torch.empty(nbytes, dtype=self.torch.uint8, device=dev)
+        self._fill_states()
+        self._call(_capi.BATCH_UPLOAD)
+        self.graph = None
+
+    # ------------------------------------------------------------------ helpers
+    def _fill_states(self):
+        for i, f in enumerate(self.fields):
+            eng = f._engine()
+            for k, name in enumerate(f._stag_components):
+                cur, nxt = eng.buffers[name]
+                self.states[i].cur[k] = cur.data_ptr()
+                self.states[i].nxt[k] = nxt.data_ptr()
+
+    def _call(self, mode):
+        lib = _capi.load()
+        store_flux = 1 if self.fields[0]._stag_family == _capi.FAMILY_ACOUSTIC else 0
+        stream = self.torch.cuda.current_stream().cuda_stream
+        code = lib.fds_stag_batch_run(self.probs, self.states, self.tables, len(self.fields),
+                                      C.c_void_p(self.workspace.data_ptr()),
+                                      self.workspace.numel(), self.step0, self.num_steps,
+                                      store_flux, mode, C.c_void_p(stream))
+        _capi.check(code)
+
+    # ------------------------------------------------------------------ phases
+    def launch(self):
+        """Enqueue the steps (kernels only) on the current stream."""
+        self._fill_states()
+        self._call(_capi.BATCH_LAUNCH)
+
+    def capture(self):
+        """Capture ``launch`` in a CUDA graph (an even step count keeps the ping-pong
+        buffers of every replay in the same place)."""
+        if self.num_steps % 2:
+            raise ValueError("graph replays need an even number of steps")
+        torch = self.torch
+        self.launch()  # warm-up outside the capture (kernel attributes, caches)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._call(_capi.BATCH_LAUNCH)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+
+    def finish(self):
+        """Record outputs into ``Output.signals`` and advance every field's step."""
+        for f, plan in zip(self.fields, self.plans):
+            eng = f._engine()
+            for name in f._stag_components:
+                getattr(f, name)._where = "device"
+            eng._last = plan
+            eng.finish(plan)
+            f.step += self.num_steps
+
+
+def simulate_batch(fields, num_steps=None, tile=None, stages=None):
+    """Advance every field by ``num_steps`` (default: the first field's
+    ``t.samples``) with one launch per step for the whole batch."""
+    if not num_steps:
+        num_steps = fields[0].t.samples
+    r = BatchRunner(fields, num_steps, tile=tile, stages=stages)
+    r.launch()
+    # the launch swapped the state pointers in `states`; mirror it in the engines
+    for i, f in enumerate(r.fields):
+        eng = f._engine()
+        for k, name in enumerate(f._stag_components):
+            bufs = eng.buffers[name]
+            if r.states[i].cur[k] != bufs[0].data_ptr():
+                bufs.reverse()
+    r.finish()
+    return r

@@ -6,6 +6,7 @@
 
 #include "fds_capi.h"
 #include "fds_internal.h"
+#include "stag_kernel.cuh"
 
 namespace fds {
 
@@ -123,6 +124,61 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
       return run_stag_f32t64(prob, state, tables, step0, nsteps, store_flux, s);
     default:
       return set_error(FDS_E_ARG, "unknown precision %d", prob->precision);
+  }
+}
+
+size_t fds_stag_batch_workspace_bytes(int32_t count, int64_t total_tiles) {
+  if (count < 0 || total_tiles < 0) return 0;
+  const size_t d = (2 * (size_t)count * sizeof(fds::StagArgs<double, double, double>) + 255) / 256 * 256;
+  return d + (size_t)total_tiles * 8;
+}
+
+int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
+                           const FdsStagTables* tables, int32_t count, void* workspace,
+                           size_t workspace_bytes, int64_t step0, int32_t nsteps,
+                           int32_t store_flux, uint32_t mode, void* stream) {
+  using namespace fds;
+  if ((mode & (FDS_BATCH_UPLOAD | FDS_BATCH_LAUNCH)) == 0 || (mode & ~3u) != 0)
+    return set_error(FDS_E_ARG, "mode must combine FDS_BATCH_UPLOAD and FDS_BATCH_LAUNCH");
+  if (!probs || !states || !tables || count < 1 || !workspace)
+    return set_error(FDS_E_ARG, "null argument or empty batch");
+  if (((uintptr_t)workspace & 255) != 0) return set_error(FDS_E_ARG, "workspace must be 256-byte aligned");
+  if (nsteps < 0 || step0 < 0) return set_error(FDS_E_ARG, "bad step range");
+  const FdsStagProblem& p0 = probs[0];
+  if (p0.family == FDS_FAMILY_ACOUSTIC && !store_flux)
+    return set_error(FDS_E_ARG, "acoustic fluxes carry state: store_flux must be set");
+  for (int i = 0; i < count; ++i) {
+    const FdsStagProblem& p = probs[i];
+    if (p.family != p0.family || p.precision != p0.precision || p.flags != p0.flags ||
+        p.tile_x != p0.tile_x || p.tile_y != p0.tile_y || p.stages != p0.stages)
+      return set_error(FDS_E_ARG, "instance %d differs from instance 0 in variant or tile", i);
+    if (p.nx < 1 || p.ny < 1) return set_error(FDS_E_ARG, "instance %d: bad grid", i);
+    if (!(p.flags & FDS_FLAG_HAS_V) || (p.flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT)))
+      return set_error(FDS_E_NOKERNEL, "batched runs cover lossless 2-D non-exact fields");
+    if (!p.coefs.bx || !p.coefs.kx) return set_error(FDS_E_ARG, "instance %d: missing coefficients", i);
+    for (int k = 0; k < 3; ++k)
+      if (!states[i].cur[k] || !states[i].nxt[k])
+        return set_error(FDS_E_ARG, "instance %d: missing state buffer %d", i, k);
+    for (int k = 0; k < 3; ++k) {
+      const FdsCompTables& t = tables[i].comp[k];
+      if (t.probe_tile_start && (!t.out || t.out_rows < nsteps))
+        return set_error(FDS_E_ARG, "instance %d: output buffer of component %d too small", i, k);
+    }
+  }
+  if (nsteps == 0) return FDS_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (p0.precision) {
+    case FDS_PREC_F64:
+      return run_batch_f64(probs, states, tables, count, workspace, workspace_bytes, step0, nsteps,
+                           store_flux, mode, s);
+    case FDS_PREC_F32:
+      return run_batch_f32(probs, states, tables, count, workspace, workspace_bytes, step0, nsteps,
+                           store_flux, mode, s);
+    case FDS_PREC_F32_T64:
+      return run_batch_f32t64(probs, states, tables, count, workspace, workspace_bytes, step0,
+                              nsteps, store_flux, mode, s);
+    default:
+      return set_error(FDS_E_ARG, "unknown precision %d", p0.precision);
   }
 }
 

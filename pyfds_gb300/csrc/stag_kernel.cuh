@@ -79,6 +79,19 @@ struct StagArgs {
   CUtensorMap tm[7];
 };
 
+// Per-launch step fields (shared by every instance of a batched launch).
+struct StepInfo {
+  int64_t step;
+  int64_t step0;
+  int32_t apply_next;
+  int32_t store_flux;
+};
+
+template <typename TP, typename TF, typename TC>
+__device__ __forceinline__ StepInfo step_of(const StagArgs<TP, TF, TC>& a) {
+  return StepInfo{a.step, a.step0, a.apply_next, a.store_flux};
+}
+
 // Variant switches of the tile kernel.
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
           bool EXACT_, int STAGES_ = 1>
@@ -403,8 +416,8 @@ __device__ __forceinline__ bool tma_finish_tile(const StagArgs<TP, TF, TC>& a, i
 // tile: inside a partial tile the owner of that slot computes it; past a full tile
 // the first TY threads compute the U column and the next TX threads the V row.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, int tile,
-                                             const StagBuf<TP, TF, TC>& b) {
+__device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, const StepInfo si,
+                                             int tile, const StagBuf<TP, TF, TC>& b) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, OY = C::OY;
   constexpr int OIT = TX * TY / NT;
   static_assert((TX & (TX - 1)) == 0, "tile width must be a power of two");
@@ -478,11 +491,11 @@ __device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, int 
   __syncthreads();
 
   // ---- flux bounds and probes (this step) ----
-  apply_bound_groups<NT>(a.tab[1], tile, sU, a.pool, a.step);
-  if constexpr (C::HAS_V) apply_bound_groups<NT>(a.tab[2], tile, sV, a.pool, a.step);
+  apply_bound_groups<NT>(a.tab[1], tile, sU, a.pool, si.step);
+  if constexpr (C::HAS_V) apply_bound_groups<NT>(a.tab[2], tile, sV, a.pool, si.step);
   __syncthreads();
-  write_probes<NT>(a.tab[1], tile, sU, a.step - a.step0);
-  if constexpr (C::HAS_V) write_probes<NT>(a.tab[2], tile, sV, a.step - a.step0);
+  write_probes<NT>(a.tab[1], tile, sU, si.step - si.step0);
+  if constexpr (C::HAS_V) write_probes<NT>(a.tab[2], tile, sV, si.step - si.step0);
 
   // ---- potential update of the owned cells ----
   TP pn[OIT];
@@ -500,7 +513,7 @@ __device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, int 
         kyi = (TF)sKy[ps];
         kyn = (TF)sKy[ps + RX];
       }
-      if (a.store_flux) {
+      if (si.store_flux) {
         a.u_out[fo[k]] = u;
         if constexpr (C::HAS_V) a.v_out[fo[k]] = v;
       }
@@ -547,11 +560,11 @@ __device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, int 
 #pragma unroll
   for (int k = 0; k < OIT; ++k)
     if (own[k]) sP[pos[k]] = pn[k];
-  if (a.apply_next) {
+  if (si.apply_next) {
     __syncthreads();
-    apply_bound_groups<NT>(a.tab[0], tile, sP, a.pool, a.step + 1);
+    apply_bound_groups<NT>(a.tab[0], tile, sP, a.pool, si.step + 1);
     __syncthreads();
-    write_probes<NT>(a.tab[0], tile, sP, a.step + 1 - a.step0);
+    write_probes<NT>(a.tab[0], tile, sP, si.step + 1 - si.step0);
 #pragma unroll
     for (int k = 0; k < OIT; ++k)
       if (own[k]) pn[k] = sP[pos[k]];
@@ -590,7 +603,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
       cp_async_wait<0>();
       __syncthreads();
     }
-    compute_tile<C>(a, t, buf0);
+    compute_tile<C>(a, step_of(a), t, buf0);
   } else {
     const StagBuf<TP, TF, TC> buf1 = carve_buffer<C, TP, TF, TC>(smem_raw + bytes, iso);
     const int stride = gridDim.x;
@@ -615,13 +628,17 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
       }
       if (tma) {
         // buffer `cur` completes once per use: its (k >> 1)-th use has parity (k >> 1) & 1
-        if (!tma_finish_tile<C>(a, t, cur ? buf1 : buf0, iso, bars + cur, (k >> 1) & 1)) return;
+        if (!tma_finish_tile<C>(a, t, cur ? buf1 : buf0, iso, bars + cur, (k >> 1) & 1)) {
+          // let a prefetch in flight into the other buffer land before leaving
+          if (tn < a.ntiles) mbar_wait(bars + (cur ^ 1), ((k + 1) >> 1) & 1, 1ll << 22);
+          return;
+        }
       } else {
         cp_async_commit();
         cp_async_wait<1>();  // this thread's copies of tile t have landed
         __syncthreads();     // ... and every other thread's
       }
-      compute_tile<C>(a, t, cur ? buf1 : buf0);
+      compute_tile<C>(a, step_of(a), t, cur ? buf1 : buf0);
     }
   }
 }

@@ -2,10 +2,13 @@
 // precision (included by one translation unit per precision).
 #pragma once
 
+#include <algorithm>
 #include <cstdio>
 #include <utility>
+#include <vector>
 
 #include "fds_internal.h"
+#include "batch_kernel.cuh"
 #include "march_kernel.cuh"
 #include "stag_kernel.cuh"
 
@@ -194,9 +197,10 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   const bool absorb = (prob->flags & FDS_FLAG_ABSORB) != 0;
   const bool axi = (prob->flags & FDS_FLAG_AXI) != 0;
   const bool exact = (prob->flags & FDS_FLAG_EXACT) != 0;
-  // stages: 0 = two-stage persistent pipeline where it is built, else one stage
+  // stages: 0 (automatic) and 1 = one CTA per tile; 2 = the persistent two-stage
+  // pipeline (built for the tile menu; measured slower on GB300 for one field)
   StagLaunch<TP, TF, TC> fn = nullptr;
-  if (prob->stages == 0 || prob->stages == 2)
+  if (prob->stages == 2)
     fn = pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi,
                                                             exact, prob->tile_x, prob->tile_y, 2);
   if (!fn && prob->stages != 2)
@@ -271,4 +275,173 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   return FDS_OK;
 }
 
+
+// ------------------------------------------------------------------ batched path
+
+inline size_t batch_desc_bytes(size_t desc_size, int32_t count) {
+  return (2 * (size_t)count * desc_size + 255) / 256 * 256;
+}
+
+// Build the descriptors and work list of one batched call for kernel variant C,
+// upload them into the caller's workspace and run the steps.
+template <class C, typename TP, typename TF, typename TC>
+int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
+                          const FdsStagTables* tables, int32_t count, void* workspace,
+                          size_t workspace_bytes, int64_t step0, int32_t nsteps,
+                          int32_t store_flux, uint32_t mode, cudaStream_t stream) {
+  using Args = StagArgs<TP, TF, TC>;
+  const size_t dbytes = batch_desc_bytes(sizeof(Args), count);
+  int64_t nwork = 0;
+  for (int i = 0; i < count; ++i) {
+    const int tx = (probs[i].nx + C::TX - 1) / C::TX, ty = (probs[i].ny + C::TY - 1) / C::TY;
+    nwork += (int64_t)tx * ty;
+  }
+  if (nwork > 0x7fffffff) return set_error(FDS_E_SIZE, "too many tiles in the batch");
+  if (dbytes + (size_t)nwork * sizeof(int2) > workspace_bytes)
+    return set_error(FDS_E_SIZE, "workspace holds %zu bytes, batch needs %zu", workspace_bytes,
+                     dbytes + (size_t)nwork * sizeof(int2));
+  Args* d_desc = (Args*)workspace;
+  int2* d_work = (int2*)((char*)workspace + dbytes);
+  cudaError_t e = cudaSuccess;
+  if (mode & FDS_BATCH_UPLOAD) {
+  std::vector<Args> desc(2 * (size_t)count);
+  std::vector<int2> work;
+  work.reserve((size_t)nwork);
+  for (int i = 0; i < count; ++i) {
+    const FdsStagProblem& pr = probs[i];
+    const FdsCoefs& c = pr.coefs;
+    const FdsStagState& st = states[i];
+    Args base{};
+    base.nx = pr.nx;
+    base.ny = pr.ny;
+    base.n = (int64_t)pr.nx * pr.ny;
+    base.tiles_x = (pr.nx + C::TX - 1) / C::TX;
+    base.ntiles = base.tiles_x * ((pr.ny + C::TY - 1) / C::TY);
+    base.bx = (const TC*)c.bx;
+    base.by = (const TC*)(c.by ? c.by : c.bx);
+    base.kx = (const TC*)c.kx;
+    base.ky = (const TC*)(c.ky ? c.ky : c.kx);
+    base.rx = (const TC*)c.rx;
+    base.iso = (base.by == base.bx && base.ky == base.kx) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) base.tab[k] = tables[i].comp[k];
+    base.pool = tables[i].pool;
+    base.status = tables[i].status;
+    bool tma = encode_tile_map(&base.tm[3], base.bx, sizeof(TC), pr.nx, pr.ny, C::RX, C::RY) &&
+               encode_tile_map(&base.tm[4], base.kx, sizeof(TC), pr.nx, pr.ny, C::RX, C::RY) &&
+               encode_tile_map(&base.tm[5], base.by, sizeof(TC), pr.nx, pr.ny, C::RX, C::RY) &&
+               encode_tile_map(&base.tm[6], base.ky, sizeof(TC), pr.nx, pr.ny, C::RX, C::RY);
+    for (int par = 0; par < 2; ++par) {
+      Args d = base;
+      void* const* in = par ? st.nxt : st.cur;
+      void* const* out = par ? st.cur : st.nxt;
+      d.p_in = (const TP*)in[0];
+      d.p_out = (TP*)out[0];
+      d.u_in = (const TF*)in[1];
+      d.u_out = (TF*)out[1];
+      d.v_in = (const TF*)in[2];
+      d.v_out = (TF*)out[2];
+      bool t = tma && encode_tile_map(&d.tm[0], in[0], sizeof(TP), pr.nx, pr.ny, C::RX, C::RY);
+      if (C::MEMORY)
+        t = t && encode_tile_map(&d.tm[1], in[1], sizeof(TF), pr.nx, pr.ny, C::RX, C::RY) &&
+            encode_tile_map(&d.tm[2], in[2], sizeof(TF), pr.nx, pr.ny, C::RX, C::RY);
+      d.use_tma = t ? 1 : 0;
+      desc[2 * (size_t)i + par] = d;
+    }
+    for (int t = 0; t < base.ntiles; ++t) work.push_back(make_int2(i, t));
+  }
+  e = cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(Args), cudaMemcpyHostToDevice,
+                      stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                        stream);
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "descriptor upload: %s", cudaGetErrorString(e));
+  }
+  if (!(mode & FDS_BATCH_LAUNCH)) return FDS_OK;
+
+  // launch configuration
+  const size_t smem = (size_t)C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(false) + 16 * C::STAGES;
+  static int optin = -1, nsm = -1, occ = -1;
+  static size_t attr = 0;
+  if (optin < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  if (smem > (size_t)optin)
+    return set_error(FDS_E_SIZE, "batched tile %dx%d needs %zu bytes of shared memory", C::TX,
+                     C::TY, smem);
+  if (smem > attr) {
+    e = cudaFuncSetAttribute(stag_batch_kernel<C, TP, TF, TC>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
+    attr = smem;
+  }
+  int grid = (int)nwork;
+  if (C::STAGES > 1) {
+    if (occ < 0) {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stag_batch_kernel<C, TP, TF, TC>,
+                                                        C::NT, smem);
+      if (e != cudaSuccess || occ < 1) occ = 1;
+    }
+    grid = (int)std::min<int64_t>(nwork, (int64_t)occ * nsm);
+  }
+  if (nsteps > 0) {
+    stag_batch_prologue_kernel<TP, TF, TC><<<count, 256, 0, stream>>>(d_desc, count, step0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch prologue: %s", cudaGetErrorString(e));
+  }
+  for (int32_t s = 0; s < nsteps; ++s) {
+    const StepInfo si{step0 + s, step0, (s + 1 < nsteps) ? 1 : 0,
+                      (store_flux || s + 1 == nsteps) ? 1 : 0};
+    stag_batch_kernel<C, TP, TF, TC><<<grid, C::NT, smem, stream>>>(d_desc, d_work, (int)nwork, si,
+                                                                    s & 1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch step: %s", cudaGetErrorString(e));
+  }
+  if (nsteps & 1)
+    for (int i = 0; i < count; ++i)
+      for (int k = 0; k < 3; ++k) std::swap(states[i].cur[k], states[i].nxt[k]);
+  return FDS_OK;
+}
+
+template <typename TP, typename TF, typename TC, bool ALLOW_ACOUSTIC>
+int32_t run_batch_typed(const FdsStagProblem* probs, FdsStagState* states,
+                        const FdsStagTables* tables, int32_t count, void* workspace,
+                        size_t workspace_bytes, int64_t step0, int32_t nsteps, int32_t store_flux,
+                        uint32_t mode, cudaStream_t stream) {
+  const FdsStagProblem& p0 = probs[0];
+  const bool acoustic = p0.family == FDS_FAMILY_ACOUSTIC;
+  const int stages = p0.stages == 2 ? 2 : 1;
+#define FDS_BATCH_TILE(TX, TY, NT)                                                              \
+  if (p0.tile_x == TX && p0.tile_y == TY) {                                                     \
+    if (acoustic) {                                                                             \
+      if constexpr (ALLOW_ACOUSTIC) {                                                           \
+        if (stages == 2)                                                                        \
+          return batch_run_variant<StagCfg<TX, TY, NT, true, true, false, false, false, 2>, TP, \
+                                   TF, TC>(probs, states, tables, count, workspace,             \
+                                           workspace_bytes, step0, nsteps, store_flux, mode,     \
+                                           stream);                                              \
+        return batch_run_variant<StagCfg<TX, TY, NT, true, true, false, false, false, 1>, TP,   \
+                                 TF, TC>(probs, states, tables, count, workspace,               \
+                                         workspace_bytes, step0, nsteps, store_flux, mode,       \
+                                         stream);                                                \
+      }                                                                                         \
+    } else {                                                                                    \
+      if (stages == 2)                                                                          \
+        return batch_run_variant<StagCfg<TX, TY, NT, true, false, false, false, false, 2>, TP,  \
+                                 TF, TC>(probs, states, tables, count, workspace,               \
+                                         workspace_bytes, step0, nsteps, store_flux, mode,       \
+                                         stream);                                                \
+      return batch_run_variant<StagCfg<TX, TY, NT, true, false, false, false, false, 1>, TP,    \
+                               TF, TC>(probs, states, tables, count, workspace,                 \
+                                       workspace_bytes, step0, nsteps, store_flux, mode,         \
+                                       stream);                                                  \
+    }                                                                                           \
+  }
+  FDS_TILE_MENU(FDS_BATCH_TILE)
+#undef FDS_BATCH_TILE
+  return set_error(FDS_E_NOKERNEL, "no batched kernel for family=%d tile=%dx%d", p0.family,
+                   p0.tile_x, p0.tile_y);
+}
 }  // namespace fds

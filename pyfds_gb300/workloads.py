@@ -123,6 +123,52 @@ def thermal2d_two_materials(n=4096, nt=50000, n_probes=64, seed=4):
             "outputs": {"temperature": [probes]}}
 
 
+def layered_media_batch(count=256, nt=2000, n_probes=16, seed=3, n_min=128, n_max=1024):
+    """``count`` Acoustic2D scenarios of uneven size and media (seeded).
+
+    Per instance: square side n = round(exp(U(ln n_min, ln n_max))); 3..8 horizontal
+    layers with uniform-random thicknesses, c ~ U[1000, 3000] m/s, rho ~ U[800, 2000]
+    kg/m^3; a point pressure source at a uniform interior cell driven by a
+    Gaussian-modulated sine with f ~ U[0.5, 5] MHz (centre 2/f, sigma 0.5/f);
+    dx = c_min / (20 f), dt = 0.4 dx / c_max; zero-pressure edges; ``n_probes``
+    pressure outputs at uniform interior cells; ``nt`` steps."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        layers = int(rng.integers(3, 9))
+        cuts = np.sort(rng.choice(np.arange(1, n), size=layers - 1, replace=False))
+        bounds = np.concatenate([[0], cuts, [n]])
+        cs = rng.uniform(1000, 3000, size=layers)
+        rhos = rng.uniform(800, 2000, size=layers)
+        f0 = rng.uniform(0.5e6, 5e6)
+        dx = cs.min() / (20 * f0)
+        dt = 0.4 * dx / cs.max()
+        t = np.arange(nt) * dt
+        xs = np.arange(n)
+        mats = [(None, {"sound_velocity": float(cs[0]), "density": float(rhos[0]),
+                        "absorption_coef": 0})]
+        for k in range(1, layers):
+            ys = np.arange(bounds[k], bounds[k + 1])
+            idx = (xs[:, None] + ys[None, :] * n).reshape(-1)
+            mats.append((idx, {"sound_velocity": float(cs[k]), "density": float(rhos[k]),
+                               "absorption_coef": 0}))
+        edges = np.unique(np.concatenate([np.arange(n), (n - 1) * n + np.arange(n),
+                                          np.arange(n) * n, np.arange(n) * n + n - 1]))
+        src = rng.integers(1, n - 1, size=2)
+        pr = rng.integers(1, n - 1, size=(n_probes, 2))
+        specs.append({
+            "kind": "Acoustic2D", "nx": n, "ny": n, "dx": dx, "dy": dx, "dt": dt, "nt": nt,
+            "steps": nt, "materials": mats,
+            "bounds": {"pressure": [
+                {"indices": edges, "value": 0, "additive": False},
+                {"indices": [int(src[0] + src[1] * n)],
+                 "value": gauss_pulse(t, f0, 2.0 / f0, 0.5 / f0), "additive": True}]},
+            "outputs": {"pressure": [(pr[:, 0] + pr[:, 1] * n).tolist()]},
+            "frequency": f0})
+    return specs
+
+
 def _material(kind, params):
     p = dict(params)
     if kind.startswith("Acoustic"):
