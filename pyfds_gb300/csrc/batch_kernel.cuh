@@ -14,28 +14,49 @@
 
 namespace fds {
 
+// Copies the core arguments of a descriptor into shared memory (a CTA reads
+// them there: stores of the tile code to global memory cannot alias them).
+template <typename TP, typename TF, typename TC>
+__device__ __forceinline__ void load_core(StagCore<TP, TF, TC>* dst,
+                                          const StagArgs<TP, TF, TC>* src) {
+  constexpr int W = sizeof(StagCore<TP, TF, TC>) / 4;
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(static_cast<const StagCore<TP, TF, TC>*>(src));
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  for (int i = threadIdx.x; i < W; i += blockDim.x) d[i] = s[i];
+}
+
+// Dynamic shared memory of the batched kernel: staging buffers (carved for the
+// anisotropic layout, the larger one), one mbarrier per stage, one core copy.
+template <class C, typename TP, typename TF, typename TC>
+__host__ __device__ constexpr size_t batch_smem_bytes() {
+  return C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(false) + 16 * C::STAGES +
+         round128(sizeof(StagCore<TP, TF, TC>));
+}
+
 template <class C, typename TP, typename TF, typename TC>
 __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     stag_batch_kernel(const StagArgs<TP, TF, TC>* __restrict__ descs, const int2* __restrict__ work,
                       int nwork, const StepInfo si, int parity) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  // every instance of one launch shares the variant; iso may differ per instance,
-  // so buffers are carved for the anisotropic (larger) layout
   const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(false);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + C::STAGES * bytes);
+  StagCore<TP, TF, TC>* core =
+      reinterpret_cast<StagCore<TP, TF, TC>*>(smem_raw + C::STAGES * bytes + 16 * C::STAGES);
   const bool aligned = (smem_addr(smem_raw) & 127u) == 0;
   if (threadIdx.x == 0)
     for (int k = 0; k < C::STAGES; ++k) mbar_init(bars + k, 1);
-  __syncthreads();
   int w = blockIdx.x;
   if constexpr (C::STAGES == 1) {
     if (w >= nwork) return;
     const int2 it = work[w];
-    const StagArgs<TP, TF, TC>& a = descs[2 * it.x + parity];
+    const StagArgs<TP, TF, TC>* d = descs + 2 * it.x + parity;
+    load_core(core, d);
+    __syncthreads();
+    const StagCore<TP, TF, TC>& a = *core;
     const bool iso = a.iso || !C::HAS_V;
     const StagBuf<TP, TF, TC> buf = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
     if (a.use_tma && aligned) {
-      if (threadIdx.x == 0) tma_issue_tile<C>(a, it.y, buf, iso, bars);
+      if (threadIdx.x == 0) tma_issue_tile<C>(a, d->tm, it.y, buf, iso, bars);
       if (!tma_finish_tile<C>(a, it.y, buf, iso, bars, 0)) return;
     } else {
       stage_tile<C>(a, it.y, buf, iso);
@@ -45,45 +66,48 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     }
     compute_tile<C>(a, si, it.y, buf);
   } else {
+    __syncthreads();
     const int stride = gridDim.x;
     uint32_t uses[2] = {0u, 0u};  // completed TMA uses of each buffer's barrier
     if (w < nwork) {
       const int2 it = work[w];
-      const StagArgs<TP, TF, TC>& a = descs[2 * it.x + parity];
-      const bool iso = a.iso || !C::HAS_V;
+      const StagArgs<TP, TF, TC>* d = descs + 2 * it.x + parity;
+      const bool iso = d->iso || !C::HAS_V;
       const StagBuf<TP, TF, TC> b0 = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
-      if (a.use_tma && aligned) {
-        if (threadIdx.x == 0) tma_issue_tile<C>(a, it.y, b0, iso, bars);
+      if (d->use_tma && aligned) {
+        if (threadIdx.x == 0) tma_issue_tile<C>(*d, d->tm, it.y, b0, iso, bars);
       } else {
-        stage_tile<C>(a, it.y, b0, iso);
+        stage_tile<C>(*d, it.y, b0, iso);
       }
     }
     cp_async_commit();
     for (int k = 0; w < nwork; ++k, w += stride) {
       const int cur = k & 1;
       const int2 it = work[w];
-      const StagArgs<TP, TF, TC>& a = descs[2 * it.x + parity];
-      const bool iso = a.iso || !C::HAS_V;
-      const StagBuf<TP, TF, TC> bc = carve_buffer<C, TP, TF, TC>(smem_raw + cur * bytes, iso);
       const int wn = w + stride;
       __syncthreads();  // every thread is done with the buffer the next copies fill
+      load_core(core, descs + 2 * it.x + parity);
+      __syncthreads();  // the whole core copy is visible before anyone reads it
       if (wn < nwork) {
         const int2 itn = work[wn];
-        const StagArgs<TP, TF, TC>& an = descs[2 * itn.x + parity];
-        const bool ison = an.iso || !C::HAS_V;
+        const StagArgs<TP, TF, TC>* dn = descs + 2 * itn.x + parity;
+        const bool ison = dn->iso || !C::HAS_V;
         const StagBuf<TP, TF, TC> bn =
             carve_buffer<C, TP, TF, TC>(smem_raw + (cur ^ 1) * bytes, ison);
-        if (an.use_tma && aligned) {
-          if (threadIdx.x == 0) tma_issue_tile<C>(an, itn.y, bn, ison, bars + (cur ^ 1));
+        if (dn->use_tma && aligned) {
+          if (threadIdx.x == 0) tma_issue_tile<C>(*dn, dn->tm, itn.y, bn, ison, bars + (cur ^ 1));
         } else {
-          stage_tile<C>(an, itn.y, bn, ison);
+          stage_tile<C>(*dn, itn.y, bn, ison);
         }
       }
       cp_async_commit();
-      if (a.use_tma && aligned) {
+      const bool tma = descs[2 * it.x + parity].use_tma && aligned;
+      const bool iso = descs[2 * it.x + parity].iso || !C::HAS_V;
+      const StagBuf<TP, TF, TC> bc = carve_buffer<C, TP, TF, TC>(smem_raw + cur * bytes, iso);
+      if (tma) {
         // barrier `cur` completes once per TMA use of its buffer (items may mix
         // TMA and cp.async staging, so the uses are counted, not derived from k)
-        if (!tma_finish_tile<C>(a, it.y, bc, iso, bars + cur, uses[cur] & 1u)) {
+        if (!tma_finish_tile<C>(*core, it.y, bc, iso, bars + cur, uses[cur] & 1u)) {
           // let a prefetch in flight into the other buffer land before leaving
           if (wn < nwork && descs[2 * work[wn].x + parity].use_tma)
             mbar_wait(bars + (cur ^ 1), uses[cur ^ 1] & 1u, 1ll << 22);
@@ -94,7 +118,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
         cp_async_wait<1>();
         __syncthreads();
       }
-      compute_tile<C>(a, si, it.y, bc);
+      compute_tile<C>(*core, si, it.y, bc);
     }
   }
 }

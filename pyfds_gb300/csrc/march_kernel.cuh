@@ -86,7 +86,7 @@ __device__ __forceinline__ T shfl_down1(T v) {
 
 // New fluxes of one row (cur*) from that row and the row above (up*).
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ void march_flux_row(const StagArgs<TP, TF, TC>& a, int y, int xl,
+__device__ __forceinline__ void march_flux_row(const StagCore<TP, TF, TC>& a, int y, int xl,
                                                bool want_x, const TP (&up_p)[C::CX],
                                                const TC (&up_by)[C::CX], const TP (&cp)[C::CX],
                                                const TF (&cuo)[C::CX], const TF (&cvo)[C::CX],
@@ -111,6 +111,11 @@ __device__ __forceinline__ void march_flux_row(const StagArgs<TP, TF, TC>& a, in
     if constexpr (C::MEMORY) {
       if (want_x) u = fma(bm, pm, fma(-b, p, cuo[k]));
       v = fma(bym, pym, fma(-by, p, cvo[k]));
+    } else if constexpr (sizeof(TP) > sizeof(TF)) {
+      // float64 potential: form the flux difference in float64 (see flux_new)
+      const TP pk = cp[k];
+      if (want_x) u = (TF)fma((TP)bm, (TP)(k == 0 ? pl : cp[k - 1]), -((TP)b * pk));
+      v = (TF)fma((TP)bym, (TP)up_p[k], -((TP)by * pk));
     } else {
       if (want_x) u = fma(bm, pm, -(b * p));
       v = fma(bym, pym, -(by * p));

@@ -43,8 +43,10 @@
 
 namespace fds {
 
+// Arguments of one field's step, without the tensor maps (the part the tile code
+// reads; a batched CTA keeps a copy of it in shared memory).
 template <typename TP, typename TF, typename TC>
-struct StagArgs {
+struct StagCore {
   int32_t nx, ny;
   int64_t n;
   int32_t tiles_x;
@@ -75,6 +77,10 @@ struct StagArgs {
   int32_t ntiles;
   int32_t use_tma;  // stage the region with TMA boxes (tm[]) instead of cp.async
   int32_t* status;  // OR-ed with kStatus* bits; may be null
+};
+
+template <typename TP, typename TF, typename TC>
+struct StagArgs : StagCore<TP, TF, TC> {
   // tensor maps of the arrays staged per tile: P, U, V, Bx, Kx, By, Ky
   CUtensorMap tm[7];
 };
@@ -88,7 +94,7 @@ struct StepInfo {
 };
 
 template <typename TP, typename TF, typename TC>
-__device__ __forceinline__ StepInfo step_of(const StagArgs<TP, TF, TC>& a) {
+__device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
   return StepInfo{a.step, a.step0, a.apply_next, a.store_flux};
 }
 
@@ -164,7 +170,7 @@ __device__ __forceinline__ void write_probes(const FdsCompTables& tb, int tile, 
 // Absorption operator a_vx_vx applied at flat index i (slot pos) to the old flux
 // held in s: diagonals sorted by offset, as scipy's todia() stores them.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ TF absorb_term(const StagArgs<TP, TF, TC>& a, const TF* s, int pos,
+__device__ __forceinline__ TF absorb_term(const StagCore<TP, TF, TC>& a, const TF* s, int pos,
                                           int64_t i) {
   TF acc = TF(0);
   if (C::HAS_V) acc = xadd(acc, xmul((TF)ldg0(a.aym, i - a.nx, a.n), s[pos - C::RX]));
@@ -176,7 +182,7 @@ __device__ __forceinline__ TF absorb_term(const StagArgs<TP, TF, TC>& a, const T
 }
 
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ TF absorb_fma(const StagArgs<TP, TF, TC>& a, const TF* s, int pos,
+__device__ __forceinline__ TF absorb_fma(const StagCore<TP, TF, TC>& a, const TF* s, int pos,
                                          int64_t i, TF acc) {
   if (C::HAS_V) acc = fma((TF)ldg0(a.aym, i - a.nx, a.n), s[pos - C::RX], acc);
   acc = fma((TF)ldg0(a.axm, i - 1, a.n), s[pos - 1], acc);
@@ -189,7 +195,7 @@ __device__ __forceinline__ TF absorb_fma(const StagArgs<TP, TF, TC>& a, const TF
 // New flux at flat index i from the potential slots (pos, pos - back) and the
 // old flux; sB holds this direction's factors (slots of out-of-range cells hold 0).
 template <class C, bool IS_X, typename TP, typename TF, typename TC>
-__device__ __forceinline__ TF flux_new(const StagArgs<TP, TF, TC>& a, const TP* sP, const TF* sF,
+__device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* sP, const TF* sF,
                                        const TC* sB, int pos, int64_t i, int x) {
   const int back = IS_X ? 1 : C::RX;
   const TF b = (TF)sB[pos];
@@ -215,7 +221,15 @@ __device__ __forceinline__ TF flux_new(const StagArgs<TP, TF, TC>& a, const TP* 
     }
   } else {
     if constexpr (!C::MEMORY) {
-      return fma(bm, pm, -(b * p));
+      if constexpr (sizeof(TP) > sizeof(TF)) {
+        // float64 potential, float32 flux: the difference of the two products is
+        // formed in float64 (near 300 K the float32 spacing, 2^-15 K, would swamp
+        // small gradients) and only the flux is rounded to float32
+        const TP bp = (TP)sB[pos] * sP[pos];
+        return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
+      } else {
+        return fma(bm, pm, -(b * p));
+      }
     } else {
       TF acc = sF[pos];
       acc = fma(-b, p, acc);
@@ -287,12 +301,12 @@ __device__ __forceinline__ void cp_async_elem(T* dst, const T* base, int64_t f, 
   const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
   const T* src = base + (ok ? f : 0);
   const int n = ok ? (int)sizeof(T) : 0;
+  // no "memory" clobber: shared memory written here is only read after
+  // cp_async_wait (which carries the clobber) and a barrier
   if constexpr (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src), "r"(n)
-                 : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src), "r"(n));
   else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(saddr), "l"(src), "r"(n)
-                 : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(saddr), "l"(src), "r"(n));
 }
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -305,28 +319,37 @@ __device__ __forceinline__ void cp_async_wait() {
 // Issue the copies of the potential, old flux and coefficients of one tile's region.
 // Slots are walked with incremental (column, row, flat index) updates.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ void stage_tile(const StagArgs<TP, TF, TC>& a, int tile,
+__device__ __forceinline__ void stage_tile(const StagCore<TP, TF, TC>& a, int tile,
                                            const StagBuf<TP, TF, TC>& b, bool iso) {
   constexpr int NT = C::NT, RX = C::RX, RN = C::RN, OY = C::OY;
   constexpr int DC = NT % RX, DR = NT / RX;
+  const int nx = a.nx;
+  const int64_t n = a.n;
+  const TP* p_in = a.p_in;
+  const TF* u_in = a.u_in;
+  const TF* v_in = a.v_in;
+  const TC* bx = a.bx;
+  const TC* kx = a.kx;
+  const TC* by = a.by;
+  const TC* ky = a.ky;
   const int x0 = (tile % a.tiles_x) * C::TX;
   const int y0 = (tile / a.tiles_x) * C::TY;
   int c = threadIdx.x % RX;
-  int64_t f = (int64_t)(y0 + (int)threadIdx.x / RX - OY) * a.nx + (x0 + c - C::OX);
-  const int64_t df = (int64_t)DR * a.nx + DC;
-  const int64_t wrap = (int64_t)a.nx - RX;
+  int64_t f = (int64_t)(y0 + (int)threadIdx.x / RX - OY) * nx + (x0 + c - C::OX);
+  const int64_t df = (int64_t)DR * nx + DC;
+  const int64_t wrap = (int64_t)nx - RX;
   for (int e = threadIdx.x; e < RN; e += NT) {
-    const bool ok = (f >= 0 && f < a.n);
-    cp_async_elem(b.P + e, a.p_in, f, ok);
+    const bool ok = (f >= 0 && f < n);
+    cp_async_elem(b.P + e, p_in, f, ok);
     if constexpr (C::MEMORY) {
-      cp_async_elem(b.U + e, a.u_in, f, ok);
-      if constexpr (C::HAS_V) cp_async_elem(b.V + e, a.v_in, f, ok);
+      cp_async_elem(b.U + e, u_in, f, ok);
+      if constexpr (C::HAS_V) cp_async_elem(b.V + e, v_in, f, ok);
     }
-    cp_async_elem(b.Bx + e, a.bx, f, ok);
-    cp_async_elem(b.Kx + e, a.kx, f, ok);
+    cp_async_elem(b.Bx + e, bx, f, ok);
+    cp_async_elem(b.Kx + e, kx, f, ok);
     if (!iso) {
-      cp_async_elem(b.By + e, a.by, f, ok);
-      cp_async_elem(b.Ky + e, a.ky, f, ok);
+      cp_async_elem(b.By + e, by, f, ok);
+      cp_async_elem(b.Ky + e, ky, f, ok);
     }
     c += DC;
     f += df;
@@ -340,8 +363,8 @@ __device__ __forceinline__ void stage_tile(const StagArgs<TP, TF, TC>& a, int ti
 // TMA staging of one tile's region: thread 0 issues one box per array into the
 // buffer, completing on `bar` (an mbarrier initialised for one arrival).
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ void tma_issue_tile(const StagArgs<TP, TF, TC>& a, int tile,
-                                               const StagBuf<TP, TF, TC>& b, bool iso,
+__device__ __forceinline__ void tma_issue_tile(const StagCore<TP, TF, TC>& a, const CUtensorMap* tm,
+                                               int tile, const StagBuf<TP, TF, TC>& b, bool iso,
                                                uint64_t* bar) {
   constexpr int RN = C::RN;
   const int gx = (tile % a.tiles_x) * C::TX - C::OX;
@@ -353,16 +376,16 @@ __device__ __forceinline__ void tma_issue_tile(const StagArgs<TP, TF, TC>& a, in
   // thread by the preceding barrier) before the asynchronous-proxy writes
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   mbar_arrive_expect_tx(bar, bytes);
-  tma_load_2d(b.P, &a.tm[0], gx, gy, bar);
+  tma_load_2d(b.P, &tm[0], gx, gy, bar);
   if constexpr (C::MEMORY) {
-    tma_load_2d(b.U, &a.tm[1], gx, gy, bar);
-    if constexpr (C::HAS_V) tma_load_2d(b.V, &a.tm[2], gx, gy, bar);
+    tma_load_2d(b.U, &tm[1], gx, gy, bar);
+    if constexpr (C::HAS_V) tma_load_2d(b.V, &tm[2], gx, gy, bar);
   }
-  tma_load_2d(b.Bx, &a.tm[3], gx, gy, bar);
-  tma_load_2d(b.Kx, &a.tm[4], gx, gy, bar);
+  tma_load_2d(b.Bx, &tm[3], gx, gy, bar);
+  tma_load_2d(b.Kx, &tm[4], gx, gy, bar);
   if (!iso) {
-    tma_load_2d(b.By, &a.tm[5], gx, gy, bar);
-    tma_load_2d(b.Ky, &a.tm[6], gx, gy, bar);
+    tma_load_2d(b.By, &tm[5], gx, gy, bar);
+    tma_load_2d(b.Ky, &tm[6], gx, gy, bar);
   }
 }
 
@@ -370,7 +393,7 @@ __device__ __forceinline__ void tma_issue_tile(const StagArgs<TP, TF, TC>& a, in
 // outside [0, nx): the box reads them as zeros, the flat-index semantics want the
 // cells of the neighbouring row. Returns false for every thread on a timeout.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ bool tma_finish_tile(const StagArgs<TP, TF, TC>& a, int tile,
+__device__ __forceinline__ bool tma_finish_tile(const StagCore<TP, TF, TC>& a, int tile,
                                                 const StagBuf<TP, TF, TC>& b, bool iso,
                                                 uint64_t* bar, uint32_t parity) {
   constexpr int RX = C::RX, RN = C::RN, OX = C::OX, OY = C::OY, NT = C::NT;
@@ -384,11 +407,19 @@ __device__ __forceinline__ bool tma_finish_tile(const StagArgs<TP, TF, TC>& a, i
     if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
     return false;
   }
-  if (x0 - OX < 0 || x0 - OX + RX > a.nx) {
-    for (int e = threadIdx.x; e < RN; e += NT) {
-      const int x = x0 - OX + e % RX;
-      if (x >= 0 && x < a.nx) continue;
-      const int64_t f = (int64_t)(y0 - OY + e / RX) * a.nx + x;
+  // box columns outside [0, nx): c in [0, clo) on the left, [chi, RX) on the right
+  const int clo = max(0, OX - x0);
+  const int chi = min(RX, a.nx - (x0 - OX));
+  const int wl = clo, wr = RX - chi;
+  if (wl + wr > 0) {
+    constexpr int RY = RN / RX;
+    for (int q = threadIdx.x; q < (wl + wr) * RY; q += NT) {
+      const int r = q / (wl + wr);
+      const int j = q - r * (wl + wr);
+      const int cc = j < wl ? j : chi + (j - wl);
+      const int e = r * RX + cc;
+      const int x = x0 - OX + cc;
+      const int64_t f = (int64_t)(y0 - OY + r) * a.nx + x;
       const bool in = (f >= 0 && f < a.n);
       b.P[e] = in ? a.p_in[f] : TP(0);
       if constexpr (C::MEMORY) {
@@ -416,7 +447,7 @@ __device__ __forceinline__ bool tma_finish_tile(const StagArgs<TP, TF, TC>& a, i
 // tile: inside a partial tile the owner of that slot computes it; past a full tile
 // the first TY threads compute the U column and the next TX threads the V row.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ void compute_tile(const StagArgs<TP, TF, TC>& a, const StepInfo si,
+__device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, const StepInfo si,
                                              int tile, const StagBuf<TP, TF, TC>& b) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, OY = C::OY;
   constexpr int OIT = TX * TY / NT;
@@ -595,7 +626,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
   __syncthreads();
   if constexpr (C::STAGES == 1) {
     if (tma) {
-      if (threadIdx.x == 0) tma_issue_tile<C>(a, t, buf0, iso, bars);
+      if (threadIdx.x == 0) tma_issue_tile<C>(a, a.tm, t, buf0, iso, bars);
       if (!tma_finish_tile<C>(a, t, buf0, iso, bars, 0)) return;
     } else {
       stage_tile<C>(a, t, buf0, iso);
@@ -609,7 +640,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     const int stride = gridDim.x;
     if (t < a.ntiles) {
       if (tma) {
-        if (threadIdx.x == 0) tma_issue_tile<C>(a, t, buf0, iso, bars);
+        if (threadIdx.x == 0) tma_issue_tile<C>(a, a.tm, t, buf0, iso, bars);
       } else {
         stage_tile<C>(a, t, buf0, iso);
       }
@@ -621,7 +652,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
       __syncthreads();  // every thread is done with the buffer the next copies fill
       if (tn < a.ntiles) {
         if (tma) {
-          if (threadIdx.x == 0) tma_issue_tile<C>(a, tn, cur ? buf0 : buf1, iso, bars + (cur ^ 1));
+          if (threadIdx.x == 0) tma_issue_tile<C>(a, a.tm, tn, cur ? buf0 : buf1, iso, bars + (cur ^ 1));
         } else {
           stage_tile<C>(a, tn, cur ? buf0 : buf1, iso);
         }

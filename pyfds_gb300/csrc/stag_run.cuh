@@ -359,7 +359,7 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
   if (!(mode & FDS_BATCH_LAUNCH)) return FDS_OK;
 
   // launch configuration
-  const size_t smem = (size_t)C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(false) + 16 * C::STAGES;
+  const size_t smem = batch_smem_bytes<C, TP, TF, TC>();
   static int optin = -1, nsm = -1, occ = -1;
   static size_t attr = 0;
   if (optin < 0) {
