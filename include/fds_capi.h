@@ -241,6 +241,28 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
                            size_t workspace_bytes, int64_t step0, int32_t nsteps,
                            int32_t store_flux, uint32_t mode, void* stream);
 
+/* Size of the scratch array built into the library for fds_stag_batch_run_static. */
+#define FDS_BATCH_STATIC_MAX_BYTES (8u << 20)
+
+/*
+ * fds_stag_batch_run without a caller-allocated workspace: the same batched run
+ * (upload and launch), with its descriptors and work list in a scratch array of
+ * FDS_BATCH_STATIC_MAX_BYTES compiled into this library. It allocates no device
+ * memory, for callers that cannot allocate (a C or Fortran host code with no
+ * device allocator of its own, or a section where an allocation is not allowed).
+ * No counterpart in the reference (pyfds has no GPU and no C interface).
+ * - A batch whose workspace (fds_stag_batch_workspace_bytes) exceeds the maximum
+ *   is rejected with FDS_E_SIZE.
+ * - The first call on each device, with that device current, looks up the
+ *   array's device address (cudaGetSymbolAddress); make that first call before
+ *   any stream capture.
+ * - Every call shares the one array: calls whose work overlaps on the GPU (other
+ *   streams, other threads) race and must be serialised by the caller.
+ */
+int32_t fds_stag_batch_run_static(const FdsStagProblem* probs, FdsStagState* states,
+                                  const FdsStagTables* tables, int32_t count, int64_t step0,
+                                  int32_t nsteps, int32_t store_flux, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

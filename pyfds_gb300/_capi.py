@@ -38,7 +38,7 @@ BOP_SIGNAL = 2
 # exported symbols, in header order
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
-                    "fds_stag_batch_run")
+                    "fds_stag_batch_run", "fds_stag_batch_run_static")
 
 
 class FdsCoefs(C.Structure):
@@ -71,6 +71,7 @@ STATUS_TMA_TIMEOUT = 1
 
 BATCH_UPLOAD = 1
 BATCH_LAUNCH = 2
+BATCH_STATIC_MAX_BYTES = 8 << 20
 
 
 # numpy mirrors of the table records (sizes asserted against the header's comments)
@@ -131,6 +132,10 @@ def load(path=None):
                                        C.POINTER(FdsStagTables), C.c_int32, C.c_void_p,
                                        C.c_size_t, C.c_int64, C.c_int32, C.c_int32, C.c_uint32,
                                        C.c_void_p]
+    lib.fds_stag_batch_run_static.restype = C.c_int32
+    lib.fds_stag_batch_run_static.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
+                                              C.POINTER(FdsStagTables), C.c_int32, C.c_int64,
+                                              C.c_int32, C.c_int32, C.c_void_p]
     v = lib.fds_abi_version()
     if v != FDS_ABI_VERSION:
         raise RuntimeError("libfdsgpu.so ABI version %d, expected %d (rebuild)" % (v, FDS_ABI_VERSION))
