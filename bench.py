@@ -308,6 +308,97 @@ def run_batched(args):
     return 0
 
 
+def _timed_simulate(spec, precision, nsteps, comp, tile=None):
+    """Run a workload on the GPU; returns ([points, steps] outputs, ms on the device)."""
+    import torch
+    from pyfds_gb300 import workloads
+    f = workloads.build_field(spec, precision=precision, tile=tile)
+    f.assemble_matrices()
+    eng = f._engine()
+    plan = eng.prepare(0, nsteps)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    eng.launch(plan)
+    e1.record(s)
+    torch.cuda.synchronize()
+    eng.finish(plan)
+    sig = np.array(getattr(f, comp).outputs[0].signals, dtype=np.float64)
+    return sig, e0.elapsed_time(e1), f.num_points
+
+
+def _errors(sig, ref, offset=0.0):
+    """Per-output relative L2 errors of sig against ref (optionally of sig - offset)."""
+    errs = []
+    for a, b in zip(sig, ref):
+        nb = np.linalg.norm(b - offset)
+        if nb > 0:
+            errs.append(float(np.linalg.norm((a - offset) - (b - offset)) / nb))
+    e = np.array(errs) if errs else np.zeros(1)
+    return {"rel_l2_max": float(e.max()), "rel_l2_median": float(np.median(e)),
+            "outputs": len(errs), "per_output": [round(x, 9) for x in errs]}
+
+
+def run_study(args):
+    """Precision study: float32 paths against the float64 GPU path (itself pinned to
+    the reference), per recorded output, with the speedup."""
+    import torch
+    from pyfds_gb300 import workloads
+    out = []
+    if args.study in ("precision", "axi"):
+        spec = workloads.axi_disc_source()
+        nt = spec["steps"]
+        ref, t64, n = _timed_simulate(spec, "f64", nt, "pressure")
+        s32, t32, _ = _timed_simulate(spec, "f32", nt, "pressure")
+        line = {"study": "Acoustic3DAxi 1024x4096 water, disc source, %d steps: f32 vs f64" % nt,
+                "f64_gcells": n * nt / t64 / 1e6, "f32_gcells": n * nt / t32 / 1e6,
+                "speedup_f32_over_f64": t64 / t32}
+        line.update(_errors(s32, ref))
+        out.append(line)
+    if args.study in ("precision", "thermal"):
+        spec = workloads.thermal2d_two_materials()
+        nt = args.time_steps or spec["steps"]
+        ref, t64, n = _timed_simulate(spec, "f64", nt, "temperature")
+        for prec in ("f32_t64", "f32"):
+            sig, tp, _ = _timed_simulate(spec, prec, nt, "temperature")
+            line = {"study": "Thermal2D 4096^2 aluminium/polymer, %d steps: %s vs f64 "
+                             "(error of the temperature rise above 293.15 K)" % (nt, prec),
+                    "f64_gcells": n * nt / t64 / 1e6, "gcells": n * nt / tp / 1e6,
+                    "speedup_over_f64": t64 / tp}
+            line.update(_errors(sig, ref, offset=293.15))
+            out.append(line)
+    if args.study in ("precision", "batched"):
+        from pyfds_gb300.batch import simulate_batch
+        specs = workloads.layered_media_batch()
+        nt = specs[0]["steps"]
+        res = {}
+        for prec in ("f64", "f32"):
+            fields = [workloads.build_field(sp, precision=prec) for sp in specs]
+            torch.cuda.synchronize()
+            import time as _t
+            t0 = _t.perf_counter()
+            simulate_batch(fields, nt, tile=(32, 32))
+            torch.cuda.synchronize()
+            res[prec] = (_t.perf_counter() - t0,
+                         [np.array(f.pressure.outputs[0].signals) for f in fields])
+        cells = sum(workloads.build_field(sp).num_points for sp in specs[:0]) or \
+            sum(sp["nx"] * sp["ny"] for sp in specs)
+        errs = [_errors(a, b)["rel_l2_max"] for a, b in zip(res["f32"][1], res["f64"][1])]
+        line = {"study": "batched layered media, %d instances x %d steps: f32 vs f64 "
+                         "(end-to-end simulate_batch)" % (len(specs), nt),
+                "f64_gcells_e2e": cells * nt / res["f64"][0] / 1e9,
+                "f32_gcells_e2e": cells * nt / res["f32"][0] / 1e9,
+                "speedup_f32_over_f64_e2e": res["f64"][0] / res["f32"][0],
+                "rel_l2_max_over_instances": float(np.max(errs)),
+                "rel_l2_median_over_instances": float(np.median(errs))}
+        out.append(line)
+    for line in out:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = _dist()
@@ -465,11 +556,15 @@ def main():
                     help="staging buffers per CTA (0: automatic)")
     ap.add_argument("--batch", type=int, default=0, help="instances of the batched workload")
     ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")
+    ap.add_argument("--study", default="", choices=["", "precision", "axi", "thermal", "batched"],
+                    help="print the precision study (float32 paths against float64) instead")
     ap.add_argument("--time-steps", type=int, default=0,
                     help="override the workload's time steps per benchmark step (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.study:
+        return run_study(args)
     if args.workload == "batched":
         return run_batched(args)
     return run_ours(args)
