@@ -108,6 +108,10 @@ typedef struct FdsStagProblem {
   int32_t stages; /* 0 (automatic) or 1: one CTA per tile; 2: persistent CTAs that
                      prefetch the next tile while computing one (lossless 2-D variants) */
   FdsCoefs coefs;
+  double offset;  /* thermal float32 only: the temperature is stored as T - offset
+                     (finer float spacing near a reference temperature); the flux
+                     adds the reference's interface term -(b_i - b_i-1) * offset, and
+                     boundary values / outputs are shifted by the caller. 0 otherwise */
 } FdsStagProblem;
 
 /*
@@ -127,7 +131,9 @@ typedef struct FdsStagState {
  * where mul is the boundary's `additive` flag as a number (True -> 1, False -> 0,
  * as the reference multiplies it in). 32 bytes. */
 typedef struct FdsBoundOp {
-  double scalar;  /* value when !(flags & FDS_BOP_SIGNAL) */
+  double scalar;  /* value when !(flags & FDS_BOP_SIGNAL); with FDS_BOP_SIGNAL a
+                     constant added to the signal sample (0 unless the potential is
+                     stored with an offset) */
   double mul;     /* factor of the old value */
   int64_t off;    /* pool offset of step 0 when FDS_BOP_SIGNAL */
   int32_t stride; /* pool stride between consecutive steps */

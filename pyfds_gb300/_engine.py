@@ -69,6 +69,7 @@ class StagEngine:
         self.table_cache = None
         self.launches = 0
         self.status = None  # device int32: FDS_STATUS_* bits reported by the kernels
+        self.offset = None  # the potential is stored as value - offset (see potential_offset)
 
     # ------------------------------------------------------------------ dtypes
     def dtypes(self):
@@ -95,9 +96,25 @@ class StagEngine:
         self.coef_key = key
 
     # ------------------------------------------------------------------- state
+    def _potential_offset(self):
+        """Offset of the stored potential: float32 thermal fields keep T - T_ref, with
+        T_ref the field's ``potential_offset`` or the mean initial temperature (the
+        float32 spacing near 0 K of deviation is fine, near 300 K it is 2^-15 K)."""
+        if self.offset is None:
+            f = self.field
+            off = getattr(f, "potential_offset", None)
+            if off is None:
+                off = 0.0
+                if f.precision == "f32" and f._stag_family == _capi.FAMILY_THERMAL:
+                    vals = np.asarray(getattr(f, f._stag_components[0])._values, dtype=np.float64)
+                    off = float(np.mean(vals)) if vals.size else 0.0
+            self.offset = float(off)
+        return self.offset
+
     def _sync_state_to_device(self, torch, dev):
         tp, tf, _ = self.dtypes()
         names = self.field._stag_components
+        off = self._potential_offset()
         memory = self.field._stag_family == _capi.FAMILY_ACOUSTIC
         for k, name in enumerate(names):
             comp = getattr(self.field, name)
@@ -115,12 +132,17 @@ class StagEngine:
                 if vals.size != n:
                     raise ValueError("component %s has %d values, field has %d points"
                                      % (name, vals.size, n))
+                if k == 0 and off:
+                    vals = vals - off
                 bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
                 comp._where = "both"
 
     def download(self, name):
         bufs = self.buffers[name]
-        return bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
+        v = bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
+        if name == self.field._stag_components[0] and self.offset:
+            v += self.offset
+        return v
 
     # ------------------------------------------------------------------ tables
     def _geometry(self):
@@ -156,7 +178,8 @@ class StagEngine:
         comps = []
         for k, name in enumerate(f._stag_components):
             comp = getattr(f, name)
-            bt = _tables.compile_bounds(comp.boundaries, n, pool, step_end, geo, k)
+            bt = _tables.compile_bounds(comp.boundaries, n, pool, step_end, geo, k,
+                                        offset=self._potential_offset() if k == 0 else 0.0)
             pt, ncols = _tables.compile_probes(comp.outputs, n, geo)
             comps.append((bt, pt, ncols))
         blob = _Blob()
@@ -230,6 +253,7 @@ class StagEngine:
         prob.tile_x = geo.tx
         prob.tile_y = geo.ty
         prob.stages = int(getattr(f, "stages", 0) or 0)
+        prob.offset = self._potential_offset()
         for name in ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx"):
             t = self.coef_tensors.get(name)
             setattr(prob.coefs, name, t.data_ptr() if t is not None else None)
@@ -281,6 +305,8 @@ class StagEngine:
             if out_t is None:
                 continue
             host = out_t.to("cpu").numpy()
+            if k == 0 and self.offset:
+                host = host + self.offset
             comp = getattr(f, name)
             for out, c0, npts in _tables.output_column_slices(comp.outputs):
                 block = host[:, c0:c0 + npts]

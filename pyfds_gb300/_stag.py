@@ -15,7 +15,8 @@ class StagField:
 
     Keyword arguments accepted by every constructor on top of the reference's:
       precision: "f64" (default, the drop-in), "f32", or "f32_t64" (thermal:
-                 float32 fluxes with a float64 temperature).
+                 float32 fluxes with a float64 temperature). Thermal "f32" stores the
+                 temperature as a float32 deviation from ``potential_offset``.
       exact:     float64 only; evaluate in the reference's operation order without
                  fused multiply-adds (bit-identical to scipy on x86-64).
       tile:      (x, y) cells per CTA for lossless 2-D fields, one of
@@ -36,6 +37,9 @@ class StagField:
         self.exact = bool(exact)
         self.tile = tuple(tile) if tile is not None else None
         self.stages = 0  # 0: automatic; 1 or 2 staging buffers (see FdsStagProblem)
+        # float32 thermal fields store T - potential_offset (None: the mean initial
+        # temperature at the first launch)
+        self.potential_offset = None
         self._stag_coefs = None
         self._flags_base = 0
         self._coef_version = 0

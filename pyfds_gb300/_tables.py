@@ -204,11 +204,17 @@ def _boundary_ops(b, n, pool, step_end):
     return cells, ops
 
 
-def compile_bounds(boundaries, n, pool, step_end, geo, role):
-    """Group/op/tile tables of one component's boundary list (None if empty)."""
+def compile_bounds(boundaries, n, pool, step_end, geo, role, offset=0.0):
+    """Group/op/tile tables of one component's boundary list (None if empty).
+
+    ``offset``: the component is stored as value - offset on the device, so every
+    operation new = mul*old + v becomes new' = mul*old' + v + (mul - 1)*offset (for
+    signal operations the constant rides in the op's ``scalar`` field)."""
     cells_l, ops_l = [], []
     for b in boundaries:
         c, o = _boundary_ops(b, n, pool, step_end)
+        if offset:
+            o["scalar"] = o["scalar"] + (o["mul"] - 1.0) * offset
         cells_l.append(c)
         ops_l.append(o)
     if not cells_l or sum(c.size for c in cells_l) == 0:

@@ -140,8 +140,9 @@ __global__ void __launch_bounds__(256) stag_batch_prologue_kernel(
       TP v = p[grp.cell];
       for (int o = grp.op_begin; o < grp.op_end; ++o) {
         const FdsBoundOp op = tb.ops[o];
-        const double val = (op.flags & FDS_BOP_SIGNAL) ? a.pool[op.off + step * (int64_t)op.stride]
-                                                       : op.scalar;
+        const double val = (op.flags & FDS_BOP_SIGNAL)
+                               ? a.pool[op.off + step * (int64_t)op.stride] + op.scalar
+                               : op.scalar;
         v = xadd(xmul((TP)op.mul, v), (TP)val);
       }
       p[grp.cell] = v;

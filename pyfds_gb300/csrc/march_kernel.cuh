@@ -117,8 +117,10 @@ __device__ __forceinline__ void march_flux_row(const StagCore<TP, TF, TC>& a, in
       if (want_x) u = (TF)fma((TP)bm, (TP)(k == 0 ? pl : cp[k - 1]), -((TP)b * pk));
       v = (TF)fma((TP)bym, (TP)up_p[k], -((TP)by * pk));
     } else {
-      if (want_x) u = fma(bm, pm, -(b * p));
-      v = fma(bym, pym, -(by * p));
+      // float32 temperature stored as T - offset (see flux_new)
+      const TF off = (TF)a.offset;
+      if (want_x) u = fma(-(b - bm), off, fma(bm, pm, -(b * p)));
+      v = fma(-(by - bym), off, fma(bym, pym, -(by * p)));
     }
     uo[k] = ok ? u : TF(0);
     vo[k] = ok ? v : TF(0);
@@ -144,7 +146,7 @@ __device__ __forceinline__ void march_bounds(const FdsCompTables& tb, int& cur, 
           for (int o = g.op_begin; o < g.op_end; ++o) {
             const FdsBoundOp op = tb.ops[o];
             const double val = (op.flags & FDS_BOP_SIGNAL)
-                                   ? pool[op.off + step * (int64_t)op.stride]
+                                   ? pool[op.off + step * (int64_t)op.stride] + op.scalar
                                    : op.scalar;
             x = xadd(xmul((T)op.mul, x), (T)val);
           }

@@ -77,6 +77,7 @@ struct StagCore {
   int32_t ntiles;
   int32_t use_tma;  // stage the region with TMA boxes (tm[]) instead of cp.async
   int32_t* status;  // OR-ed with kStatus* bits; may be null
+  double offset;    // potential stored as value - offset (thermal float32), else 0
 };
 
 template <typename TP, typename TF, typename TC>
@@ -145,8 +146,9 @@ __device__ __forceinline__ void apply_bound_groups(const FdsCompTables& tb, int 
     T v = s[grp.pos];
     for (int o = grp.op_begin; o < grp.op_end; ++o) {
       const FdsBoundOp op = tb.ops[o];
-      const double val = (op.flags & FDS_BOP_SIGNAL) ? pool[op.off + step * (int64_t)op.stride]
-                                                     : op.scalar;
+      const double val = (op.flags & FDS_BOP_SIGNAL)
+                             ? pool[op.off + step * (int64_t)op.stride] + op.scalar
+                             : op.scalar;
       v = xadd(xmul((T)op.mul, v), (T)val);
     }
     s[grp.pos] = v;
@@ -227,6 +229,10 @@ __device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* 
         // small gradients) and only the flux is rounded to float32
         const TP bp = (TP)sB[pos] * sP[pos];
         return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
+      } else if constexpr (sizeof(TF) == 4) {
+        // float32 temperature stored as T - offset: add the reference's interface
+        // term -(b - bm) * offset (zero inside a material, and when offset is 0)
+        return fma(-(b - bm), (TF)a.offset, fma(bm, pm, -(b * p)));
       } else {
         return fma(bm, pm, -(b * p));
       }
@@ -687,8 +693,9 @@ __global__ void __launch_bounds__(1024) stag_prologue_kernel(TP* p, FdsCompTable
       TP v = p[grp.cell];
       for (int o = grp.op_begin; o < grp.op_end; ++o) {
         const FdsBoundOp op = tb.ops[o];
-        const double val = (op.flags & FDS_BOP_SIGNAL) ? pool[op.off + step * (int64_t)op.stride]
-                                                       : op.scalar;
+        const double val = (op.flags & FDS_BOP_SIGNAL)
+                               ? pool[op.off + step * (int64_t)op.stride] + op.scalar
+                               : op.scalar;
         v = xadd(xmul((TP)op.mul, v), (TP)val);
       }
       p[grp.cell] = v;

@@ -236,6 +236,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   a.ex = (const TC*)c.ex;
   a.rx = (const TC*)c.rx;
   a.iso = (a.by == a.bx && a.ky == a.kx) ? 1 : 0;
+  a.offset = prob->offset;
   for (int k = 0; k < 3; ++k) a.tab[k] = tabs->comp[k];
   a.pool = tabs->pool;
   a.status = tabs->status;
@@ -323,6 +324,7 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     base.ky = (const TC*)(c.ky ? c.ky : c.kx);
     base.rx = (const TC*)c.rx;
     base.iso = (base.by == base.bx && base.ky == base.kx) ? 1 : 0;
+    base.offset = pr.offset;
     for (int k = 0; k < 3; ++k) base.tab[k] = tables[i].comp[k];
     base.pool = tables[i].pool;
     base.status = tables[i].status;

@@ -227,16 +227,23 @@ def test_float32_acoustic_error_vs_float64(gpu, precision, tol):
     assert e <= tol, e
 
 
-def test_thermal_f32_t64_error_vs_float64(gpu):
+@pytest.mark.parametrize("precision,tol", [("f32_t64", 1e-4), ("f32", 1e-3)])
+def test_thermal_reduced_precision_error(gpu, precision, tol):
+    """Float32 thermal paths against the reference: relative L2 of the temperature
+    rise above 293.15 K per output (outputs the heat has reached)."""
     g = golden("thermal2d_512.npz")
     spec = apply_inputs(workloads.thermal2d_two_materials(512, 500, 64), g)
-    f = build_field(spec, precision="f32_t64")
+    f = build_field(spec, precision=precision)
     f.simulate(spec["steps"])
-    sig = np.array(f.temperature.outputs[0].signals)
-    ref = g["temperature/sig0"]
-    rise = ref - 293.15
-    err = np.linalg.norm((sig - 293.15) - rise) / np.linalg.norm(rise)
-    assert err <= 1e-2, err
+    sig = np.array(f.temperature.outputs[0].signals) - 293.15
+    ref = g["temperature/sig0"] - 293.15
+    scale = np.linalg.norm(ref, axis=1).max()
+    worst = 0.0
+    for a, b in zip(sig, ref):
+        nb = np.linalg.norm(b)
+        if nb > 1e-6 * scale:
+            worst = max(worst, np.linalg.norm(a - b) / nb)
+    assert worst <= tol, worst
 
 
 MENU = [((64, 16), 1), ((32, 32), 1), ((128, 8), 1), ((64, 32), 1), ((128, 16), 1),
