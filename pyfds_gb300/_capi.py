@@ -38,7 +38,17 @@ BOP_SIGNAL = 2
 # exported symbols, in header order
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
-                    "fds_stag_batch_run", "fds_stag_batch_run_static")
+                    "fds_stag_batch_run", "fds_stag_batch_run_static",
+                    # include/fds_surrogate.h
+                    "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
+                    "fds_conv_wgrad_max_grid", "fds_adamw", "fds_surr_pack", "fds_surr_loss",
+                    "fds_surr_loss_parts", "fds_surr_unpack", "fds_surr_compare")
+
+CONV_FWD_GELU = 0
+CONV_FWD_LINEAR = 1
+CONV_BWD_DATA = 2
+SURR_STATUS_TIMEOUT = 1
+SURR_STATUS_ALIGN = 2
 
 
 class FdsCoefs(C.Structure):
@@ -84,6 +94,39 @@ PROBE_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("col", "<i4")], align=
 assert BOUND_OP_DTYPE.itemsize == 32
 assert BOUND_GROUP_DTYPE.itemsize == 24
 assert PROBE_DTYPE.itemsize == 16
+
+
+class FdsConvArgs(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
+                ("cin", C.c_int32), ("cout", C.c_int32), ("dilation", C.c_int32),
+                ("mode", C.c_int32), ("reserved", C.c_int32),
+                ("x", C.c_void_p), ("weight", C.c_void_p), ("bias", C.c_void_p),
+                ("resid", C.c_void_p), ("zin", C.c_void_p), ("out_z", C.c_void_p),
+                ("out_h", C.c_void_p), ("out_f32", C.c_void_p), ("status", C.c_void_p)]
+
+
+class FdsWgradArgs(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
+                ("cin", C.c_int32), ("cout", C.c_int32), ("dilation", C.c_int32),
+                ("x", C.c_void_p), ("dz", C.c_void_p), ("partial", C.c_void_p),
+                ("grid", C.c_int32), ("reserved", C.c_int32), ("status", C.c_void_p)]
+
+
+class FdsAdamArgs(C.Structure):
+    _fields_ = [("cin", C.c_int32), ("cout", C.c_int32), ("nparts", C.c_int32),
+                ("step", C.c_int32), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("weight_decay", C.c_float),
+                ("grad_scale", C.c_float), ("partial", C.c_void_p), ("weight", C.c_void_p),
+                ("bias", C.c_void_p), ("m", C.c_void_p), ("v", C.c_void_p),
+                ("wfwd", C.c_void_p), ("wbwd", C.c_void_p), ("grad_out", C.c_void_p)]
+
+
+class FdsSurrData(C.Structure):
+    _fields_ = [("count", C.c_int32), ("height", C.c_int32), ("width", C.c_int32),
+                ("state_f64", C.c_int32), ("nsnap", C.c_int32), ("edge_zero_p", C.c_int32),
+                ("inst", C.c_void_p), ("snap", C.c_void_p), ("state", C.c_void_p),
+                ("media", C.c_void_p), ("freq", C.c_void_p), ("zref", C.c_void_p),
+                ("scale", C.c_void_p), ("x", C.c_void_p), ("s", C.c_void_p), ("t", C.c_void_p)]
 
 
 class FdsError(RuntimeError):
@@ -137,6 +180,30 @@ def load(path=None):
     lib.fds_stag_batch_run_static.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                               C.POINTER(FdsStagTables), C.c_int32, C.c_int64,
                                               C.c_int32, C.c_int32, C.c_void_p]
+    # include/fds_surrogate.h
+    P = C.c_void_p
+    lib.fds_conv3x3.restype = C.c_int32
+    lib.fds_conv3x3.argtypes = [C.POINTER(FdsConvArgs), P]
+    lib.fds_conv_packed_elems.restype = C.c_int64
+    lib.fds_conv_packed_elems.argtypes = [C.c_int32, C.c_int32]
+    lib.fds_conv_pack.restype = C.c_int32
+    lib.fds_conv_pack.argtypes = [C.c_int32, C.c_int32, P, P, P, P]
+    lib.fds_conv3x3_wgrad.restype = C.c_int32
+    lib.fds_conv3x3_wgrad.argtypes = [C.POINTER(FdsWgradArgs), P]
+    lib.fds_conv_wgrad_max_grid.restype = C.c_int32
+    lib.fds_conv_wgrad_max_grid.argtypes = []
+    lib.fds_adamw.restype = C.c_int32
+    lib.fds_adamw.argtypes = [C.POINTER(FdsAdamArgs), P]
+    lib.fds_surr_pack.restype = C.c_int32
+    lib.fds_surr_pack.argtypes = [C.POINTER(FdsSurrData), P]
+    lib.fds_surr_loss.restype = C.c_int32
+    lib.fds_surr_loss.argtypes = [C.POINTER(FdsSurrData), P, P, P, P]
+    lib.fds_surr_loss_parts.restype = C.c_int32
+    lib.fds_surr_loss_parts.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+    lib.fds_surr_unpack.restype = C.c_int32
+    lib.fds_surr_unpack.argtypes = [C.POINTER(FdsSurrData), P, P]
+    lib.fds_surr_compare.restype = C.c_int32
+    lib.fds_surr_compare.argtypes = [C.c_int32, C.c_int32, C.c_int32, P, P, P, P, P, P]
     v = lib.fds_abi_version()
     if v != FDS_ABI_VERSION:
         raise RuntimeError("libfdsgpu.so ABI version %d, expected %d (rebuild)" % (v, FDS_ABI_VERSION))

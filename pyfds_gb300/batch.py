@@ -78,13 +78,16 @@ class BatchRunner:
         self._fill_states()
         self._call(_capi.BATCH_LAUNCH)
 
-    def capture(self):
+    def capture(self, warmup=True):
         """Capture ``launch`` in a CUDA graph (an even step count keeps the ping-pong
-        buffers of every replay in the same place)."""
+        buffers of every replay in the same place). The warm-up launch before the
+        capture (kernel attributes, caches) advances the fields; ``warmup=False``
+        skips it, for a process that has already launched this kernel variant."""
         if self.num_steps % 2:
             raise ValueError("graph replays need an even number of steps")
         torch = self.torch
-        self.launch()  # warm-up outside the capture (kernel attributes, caches)
+        if warmup:
+            self.launch()
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):

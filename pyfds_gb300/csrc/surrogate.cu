@@ -1,0 +1,943 @@
+// Learned-surrogate kernels: BF16 3x3 (dilated) convolutions as implicit GEMMs on
+// the fifth-generation tensor cores, their weight gradients, a fused AdamW step,
+// and the packing of solver states into network inputs.
+//
+// Convolution (forward and data gradient), per CTA tile of kRows output rows x 128
+// pixels of one image:
+//   * TMA copies, per group of 8 input channels, kRows + 2 input rows of 128 + 2d
+//     pixels (zero-filled outside the image: the convolution's padding) into a
+//     "slab" [row][pixel][8 channels] of shared memory. A slab row of 8 pixels is
+//     one 8 x 16-byte core matrix, so the A operand (128 pixels x 16 channels,
+//     K-major) of any tap (dy, dx) is the same slab pair at a start address moved
+//     by ((r + dy) * pitch + dx * d) * 16 bytes: no im2col copy.
+//   * The packed weights of the layer stay in shared memory for the whole kernel.
+//   * One thread issues 9 taps x cin/16 MMAs (M = 128, N = cout, K = 16) per output
+//     row into a tensor-memory accumulator; two accumulator sets and two staging
+//     buffers let the copies of the next tile and the epilogue of the previous one
+//     overlap the MMAs of the current one.
+//   * The epilogue (all 8 warps; warp w reads tensor-memory lanes 32 (w % 4) ..
+//     + 31, half of the columns) adds bias / residual, applies GELU or its
+//     derivative and stores bf16 (or float32).
+// Weight gradient: D[co][ci] (M = 64 >= cout, N = cin) summed over pixels per tap,
+// with both operands MN-major (channel-contiguous activations used as they are).
+//
+// Every wait on an mbarrier is bounded; a CTA that gives up records
+// FDS_SURR_STATUS_TIMEOUT, waits (bounded) for its copies and MMAs in flight,
+// frees its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include "fds_internal.h"
+#include "fds_surrogate.h"
+#include "umma.cuh"
+
+namespace fds {
+namespace surr {
+
+constexpr int kTilePx = 128;   // pixels per tile row (M of the forward MMA)
+constexpr int kRows = 4;       // output rows per forward tile
+constexpr int kWRows = 2;      // output rows per weight-gradient tile
+constexpr int kThreads = 256;  // 8 warps
+constexpr int kTmemCols = 512;
+constexpr int kAccStride = 64;  // tensor-memory columns per forward accumulator
+constexpr long long kWaitLimit = 1ll << 22;
+constexpr int kMaxSmem = 232448;  // 227 KB opt-in per CTA
+// Every launch requests all of it: one CTA holds an SM (and its 512 tensor-memory
+// columns) alone, and every operand address an MMA can form from a descriptor of
+// this kernel stays inside the CTA's shared memory.
+constexpr int kMinSmem = kMaxSmem;
+
+__host__ __device__ constexpr int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// GELU, tanh form: 0.5 v (1 + tanh(sqrt(2/pi) (v + 0.044715 v^3))).
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluA = 0.7978845608028654f;  // sqrt(2 / pi)
+constexpr float kGeluB = 0.044715f;
+__device__ __forceinline__ float gelu(float v) {
+  const float t = tanh_approx(kGeluA * fmaf(kGeluB * v * v, v, v));
+  return 0.5f * v * (1.0f + t);
+}
+__device__ __forceinline__ float gelu_grad(float v) {
+  const float t = tanh_approx(kGeluA * fmaf(kGeluB * v * v, v, v));
+  return 0.5f * (1.0f + t) + 0.5f * v * (1.0f - t * t) * kGeluA * fmaf(3.0f * kGeluB, v * v, 1.0f);
+}
+
+__device__ __forceinline__ void unpack8(const uint4& u, float (&f)[8]) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 v = __bfloat1622float2(h[i]);
+    f[2 * i] = v.x;
+    f[2 * i + 1] = v.y;
+  }
+}
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+  uint4 u;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+  return u;
+}
+
+// Packed operand index of weight (tap, co, ci): per (tap, 16-channel chunk of ci)
+// a K-major N x 16 block [ci half][co][8].
+__host__ __device__ __forceinline__ int64_t packed_index(int tap, int co, int ci, int cin,
+                                                         int cout) {
+  const int kc = ci >> 4, kh = (ci >> 3) & 1;
+  return ((int64_t)((tap * (cin >> 4) + kc) * 2 + kh) * cout + co) * 8 + (ci & 7);
+}
+
+struct Tile {
+  int b, y0, x0;  // output row r is y0 + r * dil; staged row k is y0 + (k - 1) * dil
+};
+
+// Tiles: images x row blocks of rows * dil rows x dil phases x 128-pixel columns.
+__device__ __forceinline__ Tile decode_tile(int t, int H, int W, int dil, int rows) {
+  const int nxq = W / kTilePx;
+  const int xq = t % nxq;
+  t /= nxq;
+  const int j = t % dil;
+  t /= dil;
+  const int nyb = H / (rows * dil);
+  const int yb = t % nyb;
+  return {t / nyb, yb * rows * dil + j, xq * kTilePx};
+}
+
+// Stages `nrows` input rows (spaced dil, the first one row above output row 0)
+// of `ngroups` 8-channel groups into slabs `slab` bytes apart.
+__device__ __forceinline__ void issue_rows(const CUtensorMap* map, const Tile& tl, int dil,
+                                           int ngroups, int nrows, int rx, int pitch, int slab,
+                                           int row_shift, unsigned char* dst, uint64_t* bar) {
+  for (int g = 0; g < ngroups; ++g)
+    for (int k = 0; k < nrows; ++k)
+      tma_load_4d(dst + g * slab + k * pitch * 16, map, g * 8, tl.x0 - (rx - kTilePx) / 2,
+                  tl.y0 + (k - row_shift) * dil, tl.b, bar);
+}
+
+struct ConvDev {
+  const __nv_bfloat16* w;
+  const float* bias;
+  const __nv_bfloat16* resid;
+  const __nv_bfloat16* zin;
+  __nv_bfloat16* out_z;
+  __nv_bfloat16* out_h;
+  float* out_f32;
+  int32_t* status;
+  int B, H, W, cin, cout, dil, mode, ntiles;
+  int rx, pitch, slab, abuf, wbytes;
+};
+
+__device__ void conv_epilogue(const ConvDev& p, const Tile& tl, uint32_t tacc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = warp & 3, half = warp >> 2;
+  const int hc = p.cout / 2;
+  const int x = tl.x0 + 32 * q + lane;
+  for (int r = 0; r < kRows; ++r) {
+    const int y = tl.y0 + r * p.dil;
+    const size_t pix = ((size_t)tl.b * p.H + y) * p.W + x;
+    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 8) {
+      float v[8];
+      tmem_ld8(tacc + ((uint32_t)(32 * q) << 16) + r * kAccStride + c0, v);
+      const size_t o = pix * p.cout + c0;
+      if (p.mode == FDS_CONV_FWD_LINEAR) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+        float4* dst = reinterpret_cast<float4*>(p.out_f32 + o);
+        dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+        dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+      } else if (p.mode == FDS_CONV_FWD_GELU) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+        if (p.out_z) *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
+        float res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (p.resid) unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = gelu(v[i]) + res[i];
+        *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
+      } else {  // FDS_CONV_BWD_DATA
+        if (p.resid) {
+          float res[8];
+          unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] += res[i];
+        }
+        if (p.out_h) *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
+        float z[8];
+        unpack8(*reinterpret_cast<const uint4*>(p.zin + o), z);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] *= gelu_grad(z[i]);
+        *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    conv3x3_kernel(const __grid_constant__ CUtensorMap xmap, const ConvDev p) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char* abuf0 = sm + round_up(p.wbytes, 128);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(abuf0 + 2 * p.abuf);  // tma[2], mma[2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  if ((smem_addr(sm) & 127u) != 0) {  // TMA destinations need 128-byte alignment
+    if (tid == 0 && p.status) atomicOr(p.status, FDS_SURR_STATUS_ALIGN);
+    return;
+  }
+
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i) mbar_init(bars + i, 1);
+    *abort_flag = 0;
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(p.w);
+    uint4* dst = reinterpret_cast<uint4*>(sm);
+    for (int i = tid; i < p.wbytes / 16; i += blockDim.x) dst[i] = src[i];
+  }
+  // weights written by the generic proxy are read by the tensor core (async proxy)
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = *tmem_slot;
+  const uint32_t w_addr = smem_addr(sm);
+  const int grid = gridDim.x;
+  const int KC = p.cin / 16;
+  const uint32_t idesc = umma_idesc_bf16(128, p.cout);
+  const uint32_t tx_bytes = (uint32_t)((p.cin / 8) * (kRows + 2) * p.rx * 16);
+
+  // thread 0's bookkeeping of the copies and MMAs it issued per buffer
+  int tma_issued[2] = {0, 0}, tma_seen[2] = {0, 0};
+  int mma_issued[2] = {0, 0}, mma_seen[2] = {0, 0};
+
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s) {
+      const int t = blockIdx.x + s * grid;
+      if (t < p.ntiles) {
+        mbar_arrive_expect_tx(bars + s, tx_bytes);
+        issue_rows(&xmap, decode_tile(t, p.H, p.W, p.dil, kRows), p.dil, p.cin / 8, kRows + 2,
+                   p.rx, p.pitch, p.slab, 1, abuf0 + s * p.abuf, bars + s);
+        ++tma_issued[s];
+      }
+    }
+  }
+  int k = 0;
+  Tile prev{0, 0, 0};
+  for (int t = blockIdx.x; t < p.ntiles; t += grid, ++k) {
+    const int s = k & 1;
+    if (tid == 0) {
+      if (!mbar_wait(bars + s, (uint32_t)((k >> 1) & 1), kWaitLimit)) {
+        *abort_flag = 1;
+      } else {
+        ++tma_seen[s];
+        tc_fence_after();
+        const uint32_t a0 = smem_addr(abuf0 + s * p.abuf);
+        const uint32_t acc0 = tm + (uint32_t)(s * kRows * kAccStride);
+        for (int r = 0; r < kRows; ++r) {
+          uint32_t accumulate = 0;
+          for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+            for (int kc = 0; kc < KC; ++kc) {
+              const uint32_t a =
+                  a0 + (uint32_t)(2 * kc * p.slab + ((r + dy) * p.pitch + dx * p.dil) * 16);
+              const uint32_t b = w_addr + (uint32_t)((tap * KC + kc) * p.cout * 32);
+              umma_bf16(acc0 + r * kAccStride, umma_desc(a, (uint32_t)p.slab, 128u),
+                        umma_desc(b, (uint32_t)(p.cout * 16), 128u), idesc, accumulate);
+              accumulate = 1;
+            }
+          }
+        }
+        umma_commit(bars + 2 + s);
+        ++mma_issued[s];
+      }
+    }
+    if (k > 0) {
+      const int ps = s ^ 1;
+      const bool done = mbar_wait(bars + 2 + ps, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit);
+      if (!done) *abort_flag = 1;
+      tc_fence_after();
+      if (tid == 0 && done) {
+        ++mma_seen[ps];
+        // tile k-1's MMAs are complete: its staging buffer takes tile k+1
+        if (t + grid < p.ntiles && !*abort_flag) {
+          mbar_arrive_expect_tx(bars + ps, tx_bytes);
+          issue_rows(&xmap, decode_tile(t + grid, p.H, p.W, p.dil, kRows), p.dil, p.cin / 8,
+                     kRows + 2, p.rx, p.pitch, p.slab, 1, abuf0 + ps * p.abuf, bars + ps);
+          ++tma_issued[ps];
+        }
+      }
+      if (done) conv_epilogue(p, prev, tm + (uint32_t)(ps * kRows * kAccStride));
+    }
+    prev = decode_tile(t, p.H, p.W, p.dil, kRows);
+    tc_fence_before();
+    __syncthreads();
+    if (*abort_flag) break;
+  }
+  if (!*abort_flag && k > 0) {
+    const int ls = (k - 1) & 1;
+    if (mbar_wait(bars + 2 + ls, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit)) {
+      tc_fence_after();
+      if (tid == 0) ++mma_seen[ls];
+      conv_epilogue(p, prev, tm + (uint32_t)(ls * kRows * kAccStride));
+    } else {
+      *abort_flag = 1;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
+    if (p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
+    // let every copy and MMA this CTA issued land before its memory goes away
+    for (int s = 0; s < 2; ++s) {
+      for (int u = tma_seen[s]; u < tma_issued[s]; ++u)
+        mbar_wait(bars + s, (uint32_t)(u & 1), kWaitLimit);
+      for (int u = mma_seen[s]; u < mma_issued[s]; ++u)
+        mbar_wait(bars + 2 + s, (uint32_t)(u & 1), kWaitLimit);
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tm, kTmemCols);
+}
+
+// ------------------------------------------------------------------ weight gradient
+
+struct WgradDev {
+  float* partial;
+  int32_t* status;
+  int B, H, W, cin, cout, dil, ntiles;
+  int rx, pitch, xslab, dzslab, xbytes, buf;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    wgrad_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dzmap,
+                 const WgradDev p) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * p.buf);  // tma[2], mma[2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  float* dbw = reinterpret_cast<float*>(tmem_slot + 4);  // [8 warps][64] bias partials
+  if ((smem_addr(sm) & 127u) != 0) {  // TMA destinations need 128-byte alignment
+    if (tid == 0 && p.status) atomicOr(p.status, FDS_SURR_STATUS_ALIGN);
+    return;
+  }
+
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i) mbar_init(bars + i, 1);
+    *abort_flag = 0;
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = *tmem_slot;
+  const int grid = gridDim.x;
+  const int KGx = p.cin / 8, KGz = p.cout / 8;
+  const uint32_t idesc = umma_idesc_bf16(64, p.cin) | kUmmaAMajorMN | kUmmaBMajorMN;
+  const uint32_t tx_bytes =
+      (uint32_t)(KGx * (kWRows + 2) * p.rx * 16 + KGz * kWRows * kTilePx * 16);
+  const size_t row_len = (size_t)9 * p.cout * p.cin + p.cout;
+  float* out = p.partial + (size_t)blockIdx.x * row_len;
+
+  float db[48];
+#pragma unroll
+  for (int i = 0; i < 48; ++i) db[i] = 0.0f;
+
+  int tma_issued[2] = {0, 0}, tma_seen[2] = {0, 0};
+  int mma_issued[2] = {0, 0}, mma_seen[2] = {0, 0};
+  auto issue = [&](int t, int s) {
+    const Tile tl = decode_tile(t, p.H, p.W, p.dil, kWRows);
+    unsigned char* base = sm + s * p.buf;
+    mbar_arrive_expect_tx(bars + s, tx_bytes);
+    issue_rows(&xmap, tl, p.dil, KGx, kWRows + 2, p.rx, p.pitch, p.xslab, 1, base, bars + s);
+    issue_rows(&dzmap, tl, p.dil, KGz, kWRows, kTilePx, kTilePx, p.dzslab, 0, base + p.xbytes,
+               bars + s);
+    ++tma_issued[s];
+  };
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s)
+      if (blockIdx.x + s * grid < p.ntiles) issue(blockIdx.x + s * grid, s);
+  }
+  int k = 0;
+  for (int t = blockIdx.x; t < p.ntiles; t += grid, ++k) {
+    const int s = k & 1;
+    const bool ready = mbar_wait(bars + s, (uint32_t)((k >> 1) & 1), kWaitLimit);
+    if (!ready) *abort_flag = 1;
+    if (tid == 0 && ready) {
+      ++tma_seen[s];
+      tc_fence_after();
+      const uint32_t xb = smem_addr(sm + s * p.buf);
+      const uint32_t zb = xb + (uint32_t)p.xbytes;
+      for (int r = 0; r < kWRows; ++r)
+        for (int w16 = 0; w16 < kTilePx / 16; ++w16) {
+          const uint32_t a = zb + (uint32_t)((r * kTilePx + w16 * 16) * 16);
+          const uint64_t ad = umma_desc(a, 128u, (uint32_t)p.dzslab);
+          for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+            const uint32_t b =
+                xb + (uint32_t)(((r + dy) * p.pitch + w16 * 16 + dx * p.dil) * 16);
+            umma_bf16(tm + (uint32_t)(tap * p.cin), ad, umma_desc(b, 128u, (uint32_t)p.xslab),
+                      idesc, (k > 0 || r > 0 || w16 > 0) ? 1u : 0u);
+          }
+        }
+      umma_commit(bars + 2 + s);
+      ++mma_issued[s];
+      if (k > 0) {
+        // tile k-1's MMAs are complete (and its bias sums were read before the last
+        // barrier): its buffer takes tile k+1
+        const int ps = s ^ 1;
+        if (mbar_wait(bars + 2 + ps, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit)) {
+          ++mma_seen[ps];
+          if (t + grid < p.ntiles) issue(t + grid, ps);
+        } else {
+          *abort_flag = 1;
+        }
+      }
+    }
+    if (ready) {
+      // bias gradient: thread = one pixel of the tile, all cout channels
+      const unsigned char* zs = sm + s * p.buf + p.xbytes + tid * 16;
+      for (int g = 0; g < KGz; ++g) {
+        float f[8];
+        unpack8(*reinterpret_cast<const uint4*>(zs + g * p.dzslab), f);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int gg = 0; gg < 6; ++gg)
+            if (gg == g) db[gg * 8 + i] += f[i];
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (*abort_flag) break;
+  }
+  // the last tile's MMAs (the one before it was waited inside the loop)
+  if (tid == 0 && !*abort_flag && k > 0) {
+    const int ls = (k - 1) & 1;
+    if (mbar_wait(bars + 2 + ls, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit))
+      ++mma_seen[ls];
+    else
+      *abort_flag = 1;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const bool failed = *abort_flag != 0;
+  if (!failed) {
+    // D row m (output channel) sits in lane 32 (m / 16) + m % 16
+    const int q = warp & 3, half = warp >> 2;
+    const int m = 16 * q + lane;
+    const int hc = p.cin / 2;
+    for (int tap = 0; tap < 9; ++tap)
+      for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 8) {
+        float v[8];
+        if (k > 0) {
+          tmem_ld8(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(tap * p.cin + c0), v);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = 0.0f;
+        }
+        if (lane < 16 && m < p.cout) {
+          float4* dst = reinterpret_cast<float4*>(out + ((size_t)tap * p.cout + m) * p.cin + c0);
+          dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+          dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
+      }
+    // bias: warp sums in a fixed order, then the 8 warp sums in warp order
+#pragma unroll
+    for (int i = 0; i < 48; ++i) {
+      float v = db[i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) dbw[warp * 64 + i] = v;
+    }
+    __syncthreads();
+    if (tid < p.cout) {
+      float v = 0.0f;
+      for (int w = 0; w < kThreads / 32; ++w) v += dbw[w * 64 + tid];
+      out[(size_t)9 * p.cout * p.cin + tid] = v;
+    }
+  } else if (tid == 0) {
+    if (p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
+    for (int s = 0; s < 2; ++s) {
+      for (int u = tma_seen[s]; u < tma_issued[s]; ++u)
+        mbar_wait(bars + s, (uint32_t)(u & 1), kWaitLimit);
+      for (int u = mma_seen[s]; u < mma_issued[s]; ++u)
+        mbar_wait(bars + 2 + s, (uint32_t)(u & 1), kWaitLimit);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tm, kTmemCols);
+}
+
+// ------------------------------------------------------------------ optimiser, packing
+
+__global__ void pack_kernel(int cin, int cout, const float* __restrict__ w,
+                            __nv_bfloat16* __restrict__ wfwd, __nv_bfloat16* __restrict__ wbwd) {
+  const int n = 9 * cout * cin;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int ci = i % cin, co = (i / cin) % cout, tap = i / (cin * cout);
+    const __nv_bfloat16 h = __float2bfloat16_rn(w[i]);
+    wfwd[packed_index(tap, co, ci, cin, cout)] = h;
+    if (wbwd) wbwd[packed_index(8 - tap, ci, co, cout, cin)] = h;
+  }
+}
+
+struct AdamDev {
+  int cin, cout, nparts;
+  float lr, beta1, beta2, eps, wd, scale, corr1, corr2_sqrt;
+  const float* partial;
+  float *w, *b, *m, *v;
+  __nv_bfloat16 *wfwd, *wbwd;
+  float* grad_out;
+};
+
+__global__ void adamw_kernel(const AdamDev a) {
+  const int nw = 9 * a.cout * a.cin, n = nw + a.cout;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float g = 0.0f;
+    for (int r = 0; r < a.nparts; ++r) g += a.partial[(size_t)r * n + i];
+    g *= a.scale;
+    if (a.grad_out) a.grad_out[i] = g;
+    if (a.lr == 0.0f) continue;
+    float* param = i < nw ? a.w + i : a.b + (i - nw);
+    float x = *param * (1.0f - a.lr * a.wd);
+    const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * g;
+    const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * g * g;
+    a.m[i] = m;
+    a.v[i] = v;
+    x -= a.lr / a.corr1 * m / (sqrtf(v) / a.corr2_sqrt + a.eps);
+    *param = x;
+    if (i < nw) {
+      const int ci = i % a.cin, co = (i / a.cin) % a.cout, tap = i / (a.cin * a.cout);
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      a.wfwd[packed_index(tap, co, ci, a.cin, a.cout)] = h;
+      if (a.wbwd) a.wbwd[packed_index(8 - tap, ci, co, a.cout, a.cin)] = h;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ data plumbing
+
+template <typename T>
+__device__ __forceinline__ const T* state_at(const FdsSurrData& d, int k, int snap_shift) {
+  const size_t plane = (size_t)d.height * d.width;
+  return reinterpret_cast<const T*>(d.state) +
+         ((size_t)d.inst[k] * d.nsnap + d.snap[k] + snap_shift) * 3 * plane;
+}
+
+// Block-wide sum (blockDim.x == 256), the same order on every call.
+__device__ __forceinline__ float block_sum(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float s = 0.0f;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < 8; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) scale_kernel(const FdsSurrData d) {
+  __shared__ float red[8];
+  const int k = blockIdx.x;
+  const size_t plane = (size_t)d.height * d.width;
+  const T* st = state_at<T>(d, k, 0);
+  const float z = d.zref[d.inst[k]];
+  float acc = 0.0f;
+  for (size_t i = threadIdx.x; i < plane; i += blockDim.x) {
+    const float pv = (float)st[i], vx = z * (float)st[plane + i], vy = z * (float)st[2 * plane + i];
+    acc += pv * pv + vx * vx + vy * vy;
+  }
+  const float s = block_sum(acc, red);
+  if (threadIdx.x == 0) d.scale[k] = sqrtf(s / (float)plane);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) pack_input_kernel(const FdsSurrData d) {
+  const size_t plane = (size_t)d.height * d.width;
+  const int k = blockIdx.y;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane) return;
+  const int inst = d.inst[k];
+  const float sc = d.scale[k];
+  const float inv = sc > 0.0f ? 1.0f / sc : 0.0f;
+  const float z = d.zref[inst];
+  const T* st = state_at<T>(d, k, 0);
+  const float* md = d.media + (size_t)inst * 2 * plane;
+  const float sp = (float)st[i] * inv, svx = z * (float)st[plane + i] * inv,
+              svy = z * (float)st[2 * plane + i] * inv;
+  float f[8] = {md[i], md[plane + i], sp, svx, svy, d.freq[inst], 0.0f, 0.0f};
+  uint4* x = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(d.x) + ((size_t)k * plane + i) * 16);
+  x[0] = pack8(f);
+  x[1] = make_uint4(0u, 0u, 0u, 0u);
+  reinterpret_cast<float4*>(d.s)[(size_t)k * plane + i] = make_float4(sp, svx, svy, 0.0f);
+  if (d.t) {
+    const T* tg = state_at<T>(d, k, 1);
+    reinterpret_cast<float4*>(d.t)[(size_t)k * plane + i] =
+        make_float4((float)tg[i] * inv, z * (float)tg[plane + i] * inv,
+                    z * (float)tg[2 * plane + i] * inv, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    loss_kernel(const FdsSurrData d, const float* __restrict__ y, __nv_bfloat16* __restrict__ dy,
+                float* __restrict__ parts, float gscale) {
+  __shared__ float red[8];
+  const size_t n = (size_t)d.count * d.height * d.width;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float err = 0.0f;
+  if (i < n) {
+    const float4 o = reinterpret_cast<const float4*>(y)[i * 4];
+    const float4 s = reinterpret_cast<const float4*>(d.s)[i];
+    const float4 t = reinterpret_cast<const float4*>(d.t)[i];
+    const float e0 = s.x + o.x - t.x, e1 = s.y + o.y - t.y, e2 = s.z + o.z - t.z;
+    err = e0 * e0 + e1 * e1 + e2 * e2;
+    float f[8] = {gscale * e0, gscale * e1, gscale * e2, 0, 0, 0, 0, 0};
+    uint4* g = reinterpret_cast<uint4*>(dy + i * 16);
+    g[0] = pack8(f);
+    g[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  const float s = block_sum(err, red);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) unpack_kernel(const FdsSurrData d, const float* __restrict__ y) {
+  const size_t plane = (size_t)d.height * d.width;
+  const int k = blockIdx.y;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= plane) return;
+  const int inst = d.inst[k];
+  const float sc = d.scale[k];
+  const float z = d.zref[inst];
+  const float4 o = reinterpret_cast<const float4*>(y)[((size_t)k * plane + i) * 4];
+  const float4 s = reinterpret_cast<const float4*>(d.s)[(size_t)k * plane + i];
+  T* st = const_cast<T*>(state_at<T>(d, k, 0));
+  float pv = (s.x + o.x) * sc;
+  const int xx = (int)(i % d.width), yy = (int)(i / d.width);
+  if (d.edge_zero_p && (xx == 0 || yy == 0 || xx == d.width - 1 || yy == d.height - 1)) pv = 0.0f;
+  st[i] = (T)pv;
+  st[plane + i] = (T)((s.y + o.y) * sc / z);
+  st[2 * plane + i] = (T)((s.z + o.z) * sc / z);
+}
+
+__global__ void __launch_bounds__(256)
+    compare_kernel(int H, int W, const int32_t* inst, const double* a, const double* b,
+                   const float* zref, double* out) {
+  __shared__ double red[8];
+  const int k = blockIdx.x;
+  const size_t plane = (size_t)H * W;
+  const int n = inst[k];
+  const double z = zref[n];
+  const double* pa = a + (size_t)n * 3 * plane;
+  const double* pb = b + (size_t)n * 3 * plane;
+  double dd = 0.0, bb = 0.0;
+  for (size_t i = threadIdx.x; i < 3 * plane; i += blockDim.x) {
+    const double wgt = i < plane ? 1.0 : z;
+    const double e = (pa[i] - pb[i]) * wgt, v = pb[i] * wgt;
+    dd += e * e;
+    bb += v * v;
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    double v = pass == 0 ? dd : bb;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < 8; ++w) s += red[w];
+      out[2 * k + pass] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 148;
+  }
+  return n;
+}
+
+// [B][H][W][C] bf16 activations; boxes of 8 channels x bw pixels x 1 row.
+bool encode_act_map(CUtensorMap* m, const void* base, int B, int H, int W, int C, int bw) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || !base || ((uintptr_t)base & 15) != 0 || bw > 256) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2,
+                                 (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)bw, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool channels_ok(int c) { return c == 16 || c == 32 || c == 48; }
+bool dil_ok(int d) { return d == 1 || d == 2 || d == 4 || d == 8; }
+bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+int32_t launch_error(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "%s: %s", what, cudaGetErrorString(e));
+  return FDS_OK;
+}
+
+int32_t set_smem(const void* fn, int bytes) {
+  const cudaError_t e =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+  if (e != cudaSuccess)
+    return set_error(FDS_E_LAUNCH, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+  (void)bytes;
+  return FDS_OK;
+}
+
+}  // namespace surr
+}  // namespace fds
+
+using namespace fds;
+using namespace fds::surr;
+
+extern "C" int64_t fds_conv_packed_elems(int32_t cin, int32_t cout) {
+  return (int64_t)9 * cin * cout;
+}
+
+extern "C" int32_t fds_conv3x3(const FdsConvArgs* a, void* stream) {
+  if (!a) return set_error(FDS_E_ARG, "null FdsConvArgs");
+  if (a->batch < 1 || a->height < 1 || a->width < 1)
+    return set_error(FDS_E_ARG, "bad activation shape %dx%dx%d", a->batch, a->height, a->width);
+  if (!channels_ok(a->cin) || !channels_ok(a->cout))
+    return set_error(FDS_E_ARG, "channels %d -> %d: each must be 16, 32 or 48", a->cin, a->cout);
+  if (!dil_ok(a->dilation)) return set_error(FDS_E_ARG, "dilation %d not in {1,2,4,8}", a->dilation);
+  if (a->width % kTilePx != 0 || a->height % (kRows * a->dilation) != 0)
+    return set_error(FDS_E_ARG, "%dx%d image: width must be a multiple of %d, height of %d",
+                     a->width, a->height, kTilePx, kRows * a->dilation);
+  if (!a->x || !a->weight || !aligned16(a->x) || !aligned16(a->weight))
+    return set_error(FDS_E_ARG, "x / weight missing or not 16-byte aligned");
+  switch (a->mode) {
+    case FDS_CONV_FWD_GELU:
+      if (!a->out_h || !aligned16(a->out_h) || (a->out_z && !aligned16(a->out_z)) ||
+          (a->resid && !aligned16(a->resid)))
+        return set_error(FDS_E_ARG, "FWD_GELU needs a 16-byte aligned out_h");
+      break;
+    case FDS_CONV_FWD_LINEAR:
+      if (!a->out_f32 || !aligned16(a->out_f32))
+        return set_error(FDS_E_ARG, "FWD_LINEAR needs a 16-byte aligned out_f32");
+      break;
+    case FDS_CONV_BWD_DATA:
+      if (!a->out_z || !a->zin || !aligned16(a->out_z) || !aligned16(a->zin) ||
+          (a->out_h && !aligned16(a->out_h)) || (a->resid && !aligned16(a->resid)))
+        return set_error(FDS_E_ARG, "BWD_DATA needs 16-byte aligned out_z and zin");
+      break;
+    default:
+      return set_error(FDS_E_ARG, "unknown convolution mode %d", a->mode);
+  }
+  ConvDev p{};
+  p.w = static_cast<const __nv_bfloat16*>(a->weight);
+  p.bias = a->bias;
+  p.resid = static_cast<const __nv_bfloat16*>(a->resid);
+  p.zin = static_cast<const __nv_bfloat16*>(a->zin);
+  p.out_z = static_cast<__nv_bfloat16*>(a->out_z);
+  p.out_h = static_cast<__nv_bfloat16*>(a->out_h);
+  p.out_f32 = a->out_f32;
+  p.status = a->status;
+  p.B = a->batch;
+  p.H = a->height;
+  p.W = a->width;
+  p.cin = a->cin;
+  p.cout = a->cout;
+  p.dil = a->dilation;
+  p.mode = a->mode;
+  p.ntiles = a->batch * (a->height / (kRows * a->dilation)) * a->dilation * (a->width / kTilePx);
+  p.rx = kTilePx + 2 * a->dilation;
+  p.pitch = round_up(p.rx, 8);
+  p.slab = (kRows + 2) * p.pitch * 16;
+  p.abuf = (a->cin / 8) * p.slab;
+  p.wbytes = 9 * a->cin * a->cout * 2;
+  const int smem = round_up(p.wbytes, 128) + 2 * p.abuf + 64;
+  if (smem > kMaxSmem)
+    return set_error(FDS_E_SIZE, "convolution %d->%d dilation %d needs %d bytes of shared memory",
+                     a->cin, a->cout, a->dilation, smem);
+  CUtensorMap map;
+  if (!encode_act_map(&map, a->x, a->batch, a->height, a->width, a->cin, p.rx))
+    return set_error(FDS_E_LAUNCH, "tensor map encoding failed for the convolution input");
+  int32_t rc = set_smem(reinterpret_cast<const void*>(conv3x3_kernel), smem);
+  if (rc != FDS_OK) return rc;
+  const int grid = p.ntiles < sm_count() ? p.ntiles : sm_count();
+  conv3x3_kernel<<<grid, kThreads, smem > kMinSmem ? smem : kMinSmem,
+                   static_cast<cudaStream_t>(stream)>>>(map, p);
+  return launch_error("conv3x3_kernel");
+}
+
+extern "C" int32_t fds_conv_wgrad_max_grid(void) { return sm_count(); }
+
+extern "C" int32_t fds_conv3x3_wgrad(const FdsWgradArgs* a, void* stream) {
+  if (!a) return set_error(FDS_E_ARG, "null FdsWgradArgs");
+  if (a->batch < 1 || a->height < 1 || a->width < 1)
+    return set_error(FDS_E_ARG, "bad activation shape");
+  if (!channels_ok(a->cin) || !channels_ok(a->cout))
+    return set_error(FDS_E_ARG, "channels %d -> %d: each must be 16, 32 or 48", a->cin, a->cout);
+  if (!dil_ok(a->dilation)) return set_error(FDS_E_ARG, "dilation %d not in {1,2,4,8}", a->dilation);
+  if (a->width % kTilePx != 0 || a->height % (kWRows * a->dilation) != 0)
+    return set_error(FDS_E_ARG, "%dx%d image: width must be a multiple of %d, height of %d",
+                     a->width, a->height, kTilePx, kWRows * a->dilation);
+  if (a->grid < 1 || a->grid > sm_count())
+    return set_error(FDS_E_ARG, "grid %d not in [1, %d]", a->grid, sm_count());
+  if (!a->x || !a->dz || !a->partial || !aligned16(a->x) || !aligned16(a->dz) ||
+      !aligned16(a->partial))
+    return set_error(FDS_E_ARG, "x / dz / partial missing or not 16-byte aligned");
+  WgradDev p{};
+  p.partial = a->partial;
+  p.status = a->status;
+  p.B = a->batch;
+  p.H = a->height;
+  p.W = a->width;
+  p.cin = a->cin;
+  p.cout = a->cout;
+  p.dil = a->dilation;
+  p.ntiles = a->batch * (a->height / (kWRows * a->dilation)) * a->dilation * (a->width / kTilePx);
+  p.rx = kTilePx + 2 * a->dilation;
+  p.pitch = round_up(p.rx, 8);
+  p.xslab = (kWRows + 2) * p.pitch * 16;
+  p.dzslab = kWRows * kTilePx * 16;
+  p.xbytes = (a->cin / 8) * p.xslab;
+  // the M = 64 operand spans 8 channel groups; the ones past cout are never used
+  p.buf = p.xbytes + 8 * p.dzslab;
+  const int smem = 2 * p.buf + 64 + 8 * 64 * 4;
+  if (smem > kMaxSmem)
+    return set_error(FDS_E_SIZE, "weight gradient %d->%d dilation %d needs %d bytes of shared memory",
+                     a->cin, a->cout, a->dilation, smem);
+  CUtensorMap xm, zm;
+  if (!encode_act_map(&xm, a->x, a->batch, a->height, a->width, a->cin, p.rx) ||
+      !encode_act_map(&zm, a->dz, a->batch, a->height, a->width, a->cout, kTilePx))
+    return set_error(FDS_E_LAUNCH, "tensor map encoding failed for the weight gradient");
+  int32_t rc = set_smem(reinterpret_cast<const void*>(wgrad_kernel), smem);
+  if (rc != FDS_OK) return rc;
+  wgrad_kernel<<<a->grid, kThreads, smem > kMinSmem ? smem : kMinSmem,
+                 static_cast<cudaStream_t>(stream)>>>(xm, zm, p);
+  return launch_error("wgrad_kernel");
+}
+
+extern "C" int32_t fds_conv_pack(int32_t cin, int32_t cout, const float* w, void* wfwd, void* wbwd,
+                                 void* stream) {
+  if (!channels_ok(cin) || !channels_ok(cout) || !w || !wfwd)
+    return set_error(FDS_E_ARG, "bad fds_conv_pack arguments");
+  pack_kernel<<<64, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      cin, cout, w, static_cast<__nv_bfloat16*>(wfwd), static_cast<__nv_bfloat16*>(wbwd));
+  return launch_error("pack_kernel");
+}
+
+extern "C" int32_t fds_adamw(const FdsAdamArgs* a, void* stream) {
+  if (!a || !channels_ok(a->cin) || !channels_ok(a->cout) || a->nparts < 1 || !a->partial ||
+      a->step < 1)
+    return set_error(FDS_E_ARG, "bad FdsAdamArgs");
+  if (a->lr != 0.0f && (!a->weight || !a->bias || !a->m || !a->v || !a->wfwd))
+    return set_error(FDS_E_ARG, "AdamW step needs weight, bias, moments and wfwd");
+  AdamDev d{};
+  d.cin = a->cin;
+  d.cout = a->cout;
+  d.nparts = a->nparts;
+  d.lr = a->lr;
+  d.beta1 = a->beta1;
+  d.beta2 = a->beta2;
+  d.eps = a->eps;
+  d.wd = a->weight_decay;
+  d.scale = a->grad_scale;
+  d.corr1 = (float)(1.0 - pow((double)a->beta1, (double)a->step));
+  d.corr2_sqrt = (float)sqrt(1.0 - pow((double)a->beta2, (double)a->step));
+  d.partial = a->partial;
+  d.w = a->weight;
+  d.b = a->bias;
+  d.m = a->m;
+  d.v = a->v;
+  d.wfwd = static_cast<__nv_bfloat16*>(a->wfwd);
+  d.wbwd = static_cast<__nv_bfloat16*>(a->wbwd);
+  d.grad_out = a->grad_out;
+  const int n = 9 * a->cout * a->cin + a->cout;
+  adamw_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(d);
+  return launch_error("adamw_kernel");
+}
+
+static int32_t check_data(const FdsSurrData* d, bool need_t) {
+  if (!d || d->count < 1 || d->height < 1 || d->width < 1 || d->nsnap < 1 || !d->inst ||
+      !d->snap || !d->state || !d->scale || !d->s || !d->zref)
+    return set_error(FDS_E_ARG, "bad FdsSurrData");
+  if (need_t && !d->t) return set_error(FDS_E_ARG, "FdsSurrData.t is required here");
+  if (!aligned16(d->s) || (d->t && !aligned16(d->t)) || (d->x && !aligned16(d->x)))
+    return set_error(FDS_E_ARG, "FdsSurrData buffers must be 16-byte aligned");
+  return FDS_OK;
+}
+
+extern "C" int32_t fds_surr_pack(const FdsSurrData* d, void* stream) {
+  int32_t rc = check_data(d, false);
+  if (rc != FDS_OK) return rc;
+  if (!d->x || !d->media || !d->freq) return set_error(FDS_E_ARG, "pack needs x, media, freq");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t plane = (size_t)d->height * d->width;
+  const dim3 grid((unsigned)((plane + 255) / 256), (unsigned)d->count);
+  if (d->state_f64) {
+    scale_kernel<double><<<d->count, 256, 0, s>>>(*d);
+    pack_input_kernel<double><<<grid, 256, 0, s>>>(*d);
+  } else {
+    scale_kernel<float><<<d->count, 256, 0, s>>>(*d);
+    pack_input_kernel<float><<<grid, 256, 0, s>>>(*d);
+  }
+  return launch_error("pack_input_kernel");
+}
+
+extern "C" int32_t fds_surr_loss_parts(int32_t count, int32_t height, int32_t width) {
+  return (int32_t)(((int64_t)count * height * width + 255) / 256);
+}
+
+extern "C" int32_t fds_surr_loss(const FdsSurrData* d, const float* y, void* dy, float* loss_parts,
+                                 void* stream) {
+  int32_t rc = check_data(d, true);
+  if (rc != FDS_OK) return rc;
+  if (!y || !dy || !loss_parts || !aligned16(y) || !aligned16(dy))
+    return set_error(FDS_E_ARG, "loss needs aligned y, dy and loss_parts");
+  const int nb = fds_surr_loss_parts(d->count, d->height, d->width);
+  const float gscale = 2.0f / (3.0f * (float)d->count * d->height * d->width);
+  loss_kernel<<<nb, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      *d, y, static_cast<__nv_bfloat16*>(dy), loss_parts, gscale);
+  return launch_error("loss_kernel");
+}
+
+extern "C" int32_t fds_surr_unpack(const FdsSurrData* d, const float* y, void* stream) {
+  int32_t rc = check_data(d, false);
+  if (rc != FDS_OK) return rc;
+  if (!y || !aligned16(y)) return set_error(FDS_E_ARG, "unpack needs an aligned y");
+  const size_t plane = (size_t)d->height * d->width;
+  const dim3 grid((unsigned)((plane + 255) / 256), (unsigned)d->count);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (d->state_f64)
+    unpack_kernel<double><<<grid, 256, 0, s>>>(*d, y);
+  else
+    unpack_kernel<float><<<grid, 256, 0, s>>>(*d, y);
+  return launch_error("unpack_kernel");
+}
+
+extern "C" int32_t fds_surr_compare(int32_t count, int32_t height, int32_t width,
+                                    const int32_t* inst, const double* a, const double* b,
+                                    const float* zref, double* out, void* stream) {
+  if (count < 1 || height < 1 || width < 1 || !inst || !a || !b || !zref || !out)
+    return set_error(FDS_E_ARG, "bad fds_surr_compare arguments");
+  compare_kernel<<<count, 256, 0, static_cast<cudaStream_t>(stream)>>>(height, width, inst, a, b,
+                                                                       zref, out);
+  return launch_error("compare_kernel");
+}

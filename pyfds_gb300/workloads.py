@@ -169,6 +169,58 @@ def layered_media_batch(count=256, nt=2000, n_probes=16, seed=3, n_min=128, n_ma
     return specs
 
 
+def surrogate_media(count, seed, n=256, nt=4096, t_src=704):
+    """``count`` Acoustic2D scenarios of the layered-media kind of
+    ``layered_media_batch`` at a fixed n x n grid, for the learned surrogate.
+
+    Same draws per instance (3..8 layers, c ~ U[1000, 3000], rho ~ U[800, 2000],
+    f ~ U[0.5, 5] MHz, point source, dx = c_min / (20 f), dt = 0.4 dx / c_max,
+    zero-pressure edges), without probes. The source pulse (centre 2/f, sigma
+    0.5/f) is cut to exactly zero from step ``t_src`` on, so every later window
+    is source-free (t_src = 704 covers centre + 5 sigma for any c_max / c_min <= 3).
+    Each spec also carries the per-cell ``c`` and ``rho`` maps ([n][n], row y)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        layers = int(rng.integers(3, 9))
+        cuts = np.sort(rng.choice(np.arange(1, n), size=layers - 1, replace=False))
+        bounds = np.concatenate([[0], cuts, [n]])
+        cs = rng.uniform(1000, 3000, size=layers)
+        rhos = rng.uniform(800, 2000, size=layers)
+        f0 = rng.uniform(0.5e6, 5e6)
+        dx = cs.min() / (20 * f0)
+        dt = 0.4 * dx / cs.max()
+        t = np.arange(nt) * dt
+        sig = gauss_pulse(t, f0, 2.0 / f0, 0.5 / f0)
+        sig[t_src:] = 0.0
+        xs = np.arange(n)
+        cmap = np.empty((n, n))
+        rmap = np.empty((n, n))
+        mats = [(None, {"sound_velocity": float(cs[0]), "density": float(rhos[0]),
+                        "absorption_coef": 0})]
+        cmap[:] = cs[0]
+        rmap[:] = rhos[0]
+        for k in range(1, layers):
+            ys = np.arange(bounds[k], bounds[k + 1])
+            idx = (xs[:, None] + ys[None, :] * n).reshape(-1)
+            mats.append((idx, {"sound_velocity": float(cs[k]), "density": float(rhos[k]),
+                               "absorption_coef": 0}))
+            cmap[bounds[k]:bounds[k + 1], :] = cs[k]
+            rmap[bounds[k]:bounds[k + 1], :] = rhos[k]
+        edges = np.unique(np.concatenate([np.arange(n), (n - 1) * n + np.arange(n),
+                                          np.arange(n) * n, np.arange(n) * n + n - 1]))
+        src = rng.integers(1, n - 1, size=2)
+        specs.append({
+            "kind": "Acoustic2D", "nx": n, "ny": n, "dx": dx, "dy": dx, "dt": dt, "nt": nt,
+            "steps": nt, "materials": mats,
+            "bounds": {"pressure": [
+                {"indices": edges, "value": 0, "additive": False},
+                {"indices": [int(src[0] + src[1] * n)], "value": sig, "additive": True}]},
+            "outputs": {},
+            "frequency": f0, "c_map": cmap, "rho_map": rmap, "t_src": t_src})
+    return specs
+
+
 def _material(kind, params):
     p = dict(params)
     if kind.startswith("Acoustic"):

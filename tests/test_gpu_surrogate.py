@@ -1,0 +1,325 @@
+"""Surrogate kernels on the GPU against the CPU oracle (oracle/surrogate_oracle.py).
+
+The first two tests are single-tile cases with 16 channels: they pin the operand
+layout of the tensor-core convolution (forward: K-major; weight gradient:
+MN-major, M = 64) before any larger case runs (run the file with -x).
+Tolerances: bf16-stored outputs 1e-2 relative L2 (bf16 has 8 significant bits),
+float32 outputs 1e-4, gradients of the whole network 3e-2 (bf16 activations and
+gradients against a float64 autograd)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import surrogate_oracle as so  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def env():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from pyfds_gb300 import _capi, surrogate
+    lib = _capi.load()
+    return {"lib": lib, "capi": _capi, "surr": surrogate, "dev": torch.device("cuda", 0)}
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _bf16(rng, shape, scale=1.0):
+    return torch.tensor(rng.standard_normal(shape) * scale, dtype=torch.float32).to(torch.bfloat16)
+
+
+def _packed(env, w):
+    cout, cin = w.shape[1], w.shape[2]
+    wt = torch.tensor(w, dtype=torch.float32, device=env["dev"])
+    wf = torch.empty(9 * cin * cout, dtype=torch.bfloat16, device=env["dev"])
+    wb = torch.empty_like(wf)
+    env["capi"].check(env["lib"].fds_conv_pack(cin, cout, _p(wt), _p(wf), _p(wb), _stream()))
+    return wf, wb
+
+
+def _conv(env, x, weight, cin, cout, dil, mode, bias=None, resid=None, zin=None, out_z=None,
+          out_h=None, out_f32=None):
+    capi = env["capi"]
+    status = torch.zeros(1, dtype=torch.int32, device=env["dev"])
+    a = capi.FdsConvArgs()
+    a.batch, a.height, a.width = x.shape[0], x.shape[1], x.shape[2]
+    a.cin, a.cout, a.dilation, a.mode = cin, cout, dil, mode
+    a.x, a.weight, a.bias, a.resid, a.zin = _p(x), _p(weight), _p(bias), _p(resid), _p(zin)
+    a.out_z, a.out_h, a.out_f32, a.status = _p(out_z), _p(out_h), _p(out_f32), _p(status)
+    capi.check(env["lib"].fds_conv3x3(C.byref(a), _stream()))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+
+
+def _wgrad(env, x, dz, cin, cout, dil, grid):
+    capi = env["capi"]
+    status = torch.zeros(1, dtype=torch.int32, device=env["dev"])
+    n = 9 * cout * cin + cout
+    part = torch.full((grid, n), float("nan"), dtype=torch.float32, device=env["dev"])
+    a = capi.FdsWgradArgs()
+    a.batch, a.height, a.width = x.shape[0], x.shape[1], x.shape[2]
+    a.cin, a.cout, a.dilation = cin, cout, dil
+    a.x, a.dz, a.partial, a.grid, a.status = _p(x), _p(dz), _p(part), grid, _p(status)
+    capi.check(env["lib"].fds_conv3x3_wgrad(C.byref(a), _stream()))
+    g = torch.empty(n, dtype=torch.float32, device=env["dev"])
+    ad = capi.FdsAdamArgs()
+    ad.cin, ad.cout, ad.nparts, ad.step = cin, cout, grid, 1
+    ad.lr, ad.grad_scale = 0.0, 1.0
+    ad.partial, ad.grad_out = _p(part), _p(g)
+    capi.check(env["lib"].fds_adamw(C.byref(ad), _stream()))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    g = g.cpu().numpy().astype(np.float64)
+    return g[:9 * cout * cin].reshape(9, cout, cin), g[9 * cout * cin:]
+
+
+def _oracle_conv(x, w, b, dil):
+    xt = torch.tensor(x.float().numpy(), dtype=torch.float64)
+    wt = torch.tensor(w, dtype=torch.float32).to(torch.bfloat16).to(torch.float64)
+    bt = torch.tensor(b, dtype=torch.float64) if b is not None else None
+    return so.conv3x3(xt, wt, bt, dil).numpy()
+
+
+def _oracle_wgrad(x, dz, cin, cout, dil):
+    xt = torch.tensor(x.float().numpy(), dtype=torch.float64)
+    dzt = torch.tensor(dz.float().numpy(), dtype=torch.float64)
+    w = torch.zeros((9, cout, cin), dtype=torch.float64, requires_grad=True)
+    (so.conv3x3(xt, w, None, dil) * dzt).sum().backward()
+    return w.grad.numpy(), dzt.sum(dim=(0, 1, 2)).numpy()
+
+
+# ------------------------------------------------------------------ layout probes
+
+def test_probe_conv_single_tile(env):
+    rng = np.random.default_rng(1)
+    x = _bf16(rng, (1, 4, 128, 16))
+    w = rng.standard_normal((9, 16, 16)) * 0.2
+    b = rng.standard_normal(16) * 0.1
+    wf, _ = _packed(env, w)
+    out = torch.full((1, 4, 128, 16), float("nan"), dtype=torch.float32, device=env["dev"])
+    bias = torch.tensor(b, dtype=torch.float32, device=env["dev"])
+    _conv(env, x.to(env["dev"]), wf, 16, 16, 1, env["capi"].CONV_FWD_LINEAR, bias=bias,
+          out_f32=out)
+    ref = _oracle_conv(x, w, b, 1)
+    assert _rel(out.cpu().numpy(), ref) < 1e-4
+
+
+def test_probe_wgrad_single_tile(env):
+    rng = np.random.default_rng(2)
+    x = _bf16(rng, (1, 2, 128, 16))
+    dz = _bf16(rng, (1, 2, 128, 16))
+    dw, db = _wgrad(env, x.to(env["dev"]), dz.to(env["dev"]), 16, 16, 1, grid=1)
+    rw, rb = _oracle_wgrad(x, dz, 16, 16, 1)
+    assert _rel(dw, rw) < 1e-4
+    assert _rel(db, rb) < 1e-4
+
+
+# ------------------------------------------------------------------ convolutions
+
+@pytest.mark.parametrize("cin,cout,dil", [(16, 48, 1), (48, 48, 2), (48, 48, 8), (48, 16, 1),
+                                          (32, 16, 4)])
+def test_conv_linear(env, cin, cout, dil):
+    rng = np.random.default_rng(10 + cin + cout + dil)
+    B, H, W = 2, 32, 256
+    x = _bf16(rng, (B, H, W, cin))
+    w = rng.standard_normal((9, cout, cin)) / np.sqrt(9 * cin)
+    b = rng.standard_normal(cout) * 0.1
+    wf, _ = _packed(env, w)
+    out = torch.full((B, H, W, cout), float("nan"), dtype=torch.float32, device=env["dev"])
+    _conv(env, x.to(env["dev"]), wf, cin, cout, dil, env["capi"].CONV_FWD_LINEAR,
+          bias=torch.tensor(b, dtype=torch.float32, device=env["dev"]), out_f32=out)
+    assert _rel(out.cpu().numpy(), _oracle_conv(x, w, b, dil)) < 1e-4
+
+
+@pytest.mark.parametrize("residual", [False, True])
+def test_conv_gelu(env, residual):
+    rng = np.random.default_rng(20 + residual)
+    B, H, W, c, dil = 2, 32, 128, 48, 4
+    x = _bf16(rng, (B, H, W, c))
+    w = rng.standard_normal((9, c, c)) / np.sqrt(9 * c)
+    b = rng.standard_normal(c) * 0.1
+    wf, _ = _packed(env, w)
+    z = torch.empty((B, H, W, c), dtype=torch.bfloat16, device=env["dev"])
+    h = torch.empty_like(z)
+    xd = x.to(env["dev"])
+    _conv(env, xd, wf, c, c, dil, env["capi"].CONV_FWD_GELU,
+          bias=torch.tensor(b, dtype=torch.float32, device=env["dev"]),
+          resid=xd if residual else None, out_z=z, out_h=h)
+    zr = _oracle_conv(x, w, b, dil)
+    hr = so.gelu(torch.tensor(zr)).numpy() + (x.float().numpy() if residual else 0.0)
+    assert _rel(z.float().cpu().numpy(), zr) < 1e-2
+    assert _rel(h.float().cpu().numpy(), hr) < 1e-2
+
+
+@pytest.mark.parametrize("cin,cout,dil,residual", [(48, 48, 8, True), (48, 16, 1, False),
+                                                   (16, 48, 2, True)])
+def test_conv_backward_data(env, cin, cout, dil, residual):
+    """dz = (conv^T(g) + resid) * gelu'(zin), with conv^T the data gradient of a
+    cin -> cout layer (run as a cout -> cin convolution on the packed wbwd)."""
+    rng = np.random.default_rng(30 + cin + dil)
+    B, H, W = 2, 32, 128
+    g = _bf16(rng, (B, H, W, cout))
+    zin = _bf16(rng, (B, H, W, cin))
+    res = _bf16(rng, (B, H, W, cin))
+    w = rng.standard_normal((9, cout, cin)) / np.sqrt(9 * cin)
+    _, wb = _packed(env, w)
+    dz = torch.empty((B, H, W, cin), dtype=torch.bfloat16, device=env["dev"])
+    dh = torch.empty_like(dz)
+    _conv(env, g.to(env["dev"]), wb, cout, cin, dil, env["capi"].CONV_BWD_DATA,
+          resid=res.to(env["dev"]) if residual else None, zin=zin.to(env["dev"]), out_z=dz,
+          out_h=dh)
+    # oracle: data gradient of y = conv(x, w) contracted with g
+    xt = torch.zeros((B, H, W, cin), dtype=torch.float64, requires_grad=True)
+    wt = torch.tensor(w, dtype=torch.float32).to(torch.bfloat16).to(torch.float64)
+    (so.conv3x3(xt, wt, None, dil) * torch.tensor(g.float().numpy(), dtype=torch.float64)).sum().backward()
+    gr = xt.grad.numpy() + (res.float().numpy() if residual else 0.0)
+    zt = torch.tensor(zin.float().numpy(), dtype=torch.float64, requires_grad=True)
+    so.gelu(zt).sum().backward()
+    assert _rel(dh.float().cpu().numpy(), gr) < 1e-2
+    assert _rel(dz.float().cpu().numpy(), gr * zt.grad.numpy()) < 1e-2
+
+
+@pytest.mark.parametrize("cin,cout,dil", [(48, 48, 8), (16, 48, 1), (48, 16, 2)])
+def test_wgrad(env, cin, cout, dil):
+    rng = np.random.default_rng(40 + cin + cout + dil)
+    B, H, W = 2, 32, 256
+    x = _bf16(rng, (B, H, W, cin))
+    dz = _bf16(rng, (B, H, W, cout))
+    grid = env["lib"].fds_conv_wgrad_max_grid()
+    dw, db = _wgrad(env, x.to(env["dev"]), dz.to(env["dev"]), cin, cout, dil, grid)
+    rw, rb = _oracle_wgrad(x, dz, cin, cout, dil)
+    assert _rel(dw, rw) < 1e-4
+    assert _rel(db, rb) < 1e-4
+
+
+# ------------------------------------------------------------------ optimiser, plumbing
+
+def test_adamw_matches_torch(env):
+    capi, lib = env["capi"], env["lib"]
+    rng = np.random.default_rng(5)
+    cin, cout, nparts = 16, 48, 3
+    n = 9 * cout * cin + cout
+    w0 = rng.standard_normal((9, cout, cin)).astype(np.float32)
+    b0 = rng.standard_normal(cout).astype(np.float32)
+    parts = rng.standard_normal((nparts, n)).astype(np.float32)
+    dev = env["dev"]
+    W = torch.tensor(w0, device=dev)
+    Bv = torch.tensor(b0, device=dev)
+    m = torch.zeros(n, device=dev)
+    v = torch.zeros(n, device=dev)
+    wf = torch.empty(9 * cin * cout, dtype=torch.bfloat16, device=dev)
+    wb = torch.empty_like(wf)
+    P = torch.tensor(parts, device=dev)
+    for step in (1, 2, 3):
+        a = capi.FdsAdamArgs()
+        a.cin, a.cout, a.nparts, a.step = cin, cout, nparts, step
+        a.lr, a.beta1, a.beta2, a.eps, a.weight_decay, a.grad_scale = 1e-2, 0.9, 0.999, 1e-8, 0.01, 1.0
+        a.partial, a.weight, a.bias, a.m, a.v = _p(P), _p(W), _p(Bv), _p(m), _p(v)
+        a.wfwd, a.wbwd = _p(wf), _p(wb)
+        capi.check(lib.fds_adamw(C.byref(a), _stream()))
+    g = parts.astype(np.float64).sum(axis=0)
+    rw, rb = so.adamw_step(w0, b0, g[:9 * cout * cin].reshape(9, cout, cin), g[9 * cout * cin:],
+                           lr=1e-2, step=3)
+    assert np.allclose(W.cpu().numpy(), rw, rtol=1e-5, atol=1e-6)
+    assert np.allclose(Bv.cpu().numpy(), rb, rtol=1e-5, atol=1e-6)
+    # the packed operand holds the updated weights
+    wf2, _ = _packed(env, W.cpu().numpy())
+    assert torch.equal(wf, wf2)
+
+
+def test_pack_and_unpack(env):
+    capi, lib, surr = env["capi"], env["lib"], env["surr"]
+    rng = np.random.default_rng(6)
+    N, n, dev = 3, 128, env["dev"]
+    state = rng.standard_normal((N, 1, 3, n, n)) * np.array([1.0, 1e-6, 1e-6])[None, None, :, None, None]
+    media = rng.uniform(0.1, 1.0, size=(N, 2, n, n)).astype(np.float32)
+    freq = rng.uniform(-1, 1, size=N).astype(np.float32)
+    zref = rng.uniform(1e6, 3e6, size=N).astype(np.float32)
+    S = torch.tensor(state, dtype=torch.float64, device=dev)
+    Mt, Ft, Zt = (torch.tensor(a, device=dev) for a in (media, freq, zref))
+    net = surr.ConvNet()
+    b = net.buffers(2, n, n, train=False)
+    inst = torch.tensor([2, 0], dtype=torch.int32, device=dev)
+    snap = torch.zeros(2, dtype=torch.int32, device=dev)
+    d = surr._surr_data(torch, S, Mt, Ft, Zt, 1, inst, snap, b, n, f64=True, target=False)
+    capi.check(lib.fds_surr_pack(C.byref(d), _stream()))
+    torch.cuda.synchronize()
+    for k, i in enumerate((2, 0)):
+        x, s, sc = so.pack_inputs(state[i, 0], media[i], freq[i], zref[i])
+        assert abs(float(b["scale"][k]) - sc) < 1e-5 * sc
+        assert _rel(b["x"][k].float().cpu().numpy(), x) < 1e-2
+        assert _rel(b["s"][k].cpu().numpy(), s) < 1e-5
+    y = torch.tensor(rng.standard_normal((2, n, n, 16)) * 0.01, dtype=torch.float32, device=dev)
+    b["y"].copy_(y)
+    capi.check(lib.fds_surr_unpack(C.byref(d), _p(b["y"]), _stream()))
+    torch.cuda.synchronize()
+    out = S.cpu().numpy()
+    for k, i in enumerate((2, 0)):
+        sc = float(b["scale"][k])
+        nv = (b["s"][k].cpu().numpy()[..., :3] + y[k].cpu().numpy()[..., :3])
+        p = nv[..., 0] * sc
+        p[0, :] = p[-1, :] = p[:, 0] = p[:, -1] = 0.0
+        assert _rel(out[i, 0, 0], p) < 1e-5
+        assert _rel(out[i, 0, 1], nv[..., 1] * sc / zref[i]) < 1e-5
+    assert np.array_equal(out[1], state[1])  # untouched instance
+
+
+# ------------------------------------------------------------------ whole network
+
+def test_network_gradients_match_oracle(env):
+    surr, capi, lib = env["surr"], env["capi"], env["lib"]
+    rng = np.random.default_rng(7)
+    B, n = 2, 32
+    W = 128
+    net = surr.ConvNet(seed=3)
+    # larger residual / output weights than the initialisation, so that every layer
+    # carries a gradient well above bf16 noise
+    ws = [(w * (1.0 if k == 0 else 4.0), rng.standard_normal(b.shape) * 0.1)
+          for k, (w, b) in enumerate(net.get_weights())]
+    net.set_weights(ws)
+    b = net.buffers(B, n, W, train=True)
+    x = _bf16(rng, (B, n, W, 16))
+    x[..., 6:] = 0
+    s = rng.standard_normal((B, n, W, 4)).astype(np.float32)
+    t = (s + rng.standard_normal((B, n, W, 4)) * 0.3).astype(np.float32)
+    s[..., 3] = t[..., 3] = 0
+    b["x"].copy_(x.to(env["dev"]))
+    b["s"].copy_(torch.tensor(s))
+    b["t"].copy_(torch.tensor(t))
+    shape = (B, n, W)
+    net.forward(b, shape, train=True)
+    d = capi.FdsSurrData()
+    d.count, d.height, d.width, d.nsnap = B, n, W, 1
+    dummy = torch.zeros(B, dtype=torch.int32, device=env["dev"])
+    d.inst = d.snap = _p(dummy)
+    d.state = _p(b["s"])
+    d.zref = _p(b["scale"])
+    d.scale, d.s, d.t = _p(b["scale"]), _p(b["s"]), _p(b["t"])
+    capi.check(lib.fds_surr_loss(C.byref(d), _p(b["y"]), _p(b["dy"]), _p(b["loss_parts"]),
+                                 _stream()))
+    net.backward(b, shape)
+    grads = net.gradients()
+    net.check_status()
+    mse = float(b["loss_parts"].sum().item()) / (3 * B * n * W)
+    L, ref = so.gradients(x.float().numpy(), s, t, net.get_weights(), net.layers)
+    assert abs(mse - L) < 2e-2 * L
+    for k, ((gw, gb), (rw, rb)) in enumerate(zip(grads, ref)):
+        assert _rel(gw, rw) < 3e-2, ("layer", k, _rel(gw, rw))
+        assert _rel(gb, rb) < 3e-2, ("layer bias", k, _rel(gb, rb))
