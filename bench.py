@@ -413,6 +413,101 @@ def run_study(args):
     return 0
 
 
+def _bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["bf16_tflops"]), float(d["bf16_tflops_sustained"]), "measured"
+    return 1900.0, 1700.0, "fallback"
+
+
+def run_surrogate(args):
+    """Learned surrogate: snapshots from the batched FP64 solver, training on the
+    GPU with the tensor-core kernels, then a rollout with FD check windows against
+    the plain FP64 batched solver on unseen media."""
+    import torch
+    from pyfds_gb300 import surrogate as S
+    from pyfds_gb300 import workloads
+    torch.cuda.init()
+    n = 256
+    t0 = time.perf_counter()
+    data = S.generate_data(args.surr_instances, args.surr_snaps, seed=11, n=n)
+    t_data = time.perf_counter() - t0
+    pairs = len(data.pairs())
+    net = S.ConvNet(seed=0)
+    # kernel throughput: one forward and one training iteration on a batch of 32
+    B = args.surr_batch
+    b = net.buffers(B, n, n, train=True)
+    shape = (B, n, n)
+    flops_fwd = sum(2 * 9 * cin * cout for cin, cout, _, _ in net.layers) * B * n * n
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(3):
+        net.forward(b, shape, train=True)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(10):
+        net.forward(b, shape, train=True)
+    ev[1].record()
+    torch.cuda.synchronize()
+    t_fwd = ev[0].elapsed_time(ev[1]) / 10 / 1e3
+    inf = net.buffers(B, n, n, train=False)
+    inf["x"].copy_(b["x"])
+    ev[2].record()
+    for _ in range(10):
+        net.forward(inf, shape, train=False)
+    ev[3].record()
+    torch.cuda.synchronize()
+    t_inf = ev[2].elapsed_time(ev[3]) / 10 / 1e3
+    b["dy"].zero_()
+    ev[0].record()
+    for _ in range(5):
+        net.backward(b, shape)
+    ev[1].record()
+    torch.cuda.synchronize()
+    t_bwd = ev[0].elapsed_time(ev[1]) / 5 / 1e3
+    net = S.ConvNet(seed=0)
+    losses, t_train = S.train(net, data, epochs=args.surr_epochs, batch=B, lr=1e-3, seed=0,
+                              log_every=max(1, pairs // B))
+    steps = len(losses) and losses[-1][0] + 1
+    del data
+    torch.cuda.empty_cache()
+    specs = workloads.surrogate_media(args.surr_eval, seed=99, n=n, nt=args.surr_steps)
+    s_fd, t_fd, = S.fd_rollout(specs, args.surr_steps)
+    torch.cuda.empty_cache()
+    s_nn, t_nn, rep = S.surrogate_rollout(net, specs, args.surr_steps, check_every=8, tol=0.01)
+    zref = S.media_tensors(specs, torch, torch.device("cuda", 0))[2]
+    idx = torch.arange(len(specs), dtype=torch.int32, device="cuda")
+    err = S.rel_l2(net, s_nn, s_fd, zref, idx)
+    peak, peak_s, how = _bf16_peak()
+    iters = steps
+    train_flops = 3 * flops_fwd * iters
+    line = {"study": "learned surrogate: 8-layer dilated residual CNN, 48 ch, bf16 tcgen05 "
+                     "kernels; %d pairs at %dx%d, K=64; eval %d unseen media x %d steps"
+                     % (pairs, n, n, len(specs), args.surr_steps),
+            "data_generation_s": t_data, "pairs": pairs,
+            "forward_ms_batch%d" % B: t_fwd * 1e3,
+            "forward_tflops": flops_fwd / t_fwd / 1e12,
+            "inference_tflops": flops_fwd / t_inf / 1e12,
+            "backward_ms_batch%d" % B: t_bwd * 1e3,
+            "backward_tflops": 2 * flops_fwd / t_bwd / 1e12,
+            "peak_bf16_tflops": peak, "peak_note": how + " (burst, cuBLAS)",
+            "train_steps": iters, "train_s": t_train,
+            "train_tflops": train_flops / t_train / 1e12,
+            "loss_first": losses[0][1] if losses else None,
+            "loss_last": losses[-1][1] if losses else None,
+            "loss_per_epoch": [l for _, l in losses],
+            "fd_rollout_s": t_fd, "surrogate_rollout_s": t_nn,
+            "speedup_vs_fd64": t_fd / t_nn,
+            "final_rel_l2_median": float(np.median(err)), "final_rel_l2_max": float(np.max(err)),
+            "final_rel_l2_p90": float(np.percentile(err, 90)),
+            "fallback_instances": rep["fallback_instances"],
+            "network_jumps": rep["network_jumps"], "solver_windows": rep["solver_windows"],
+            "checks": rep["checks"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = _dist()
@@ -570,13 +665,25 @@ def main():
                     help="staging buffers per CTA (0: automatic)")
     ap.add_argument("--batch", type=int, default=0, help="instances of the batched workload")
     ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")
-    ap.add_argument("--study", default="", choices=["", "precision", "axi", "thermal", "batched"],
-                    help="print the precision study (float32 paths against float64) instead")
+    ap.add_argument("--study", default="",
+                    choices=["", "precision", "axi", "thermal", "batched", "surrogate"],
+                    help="print the precision study (float32 paths against float64) or the "
+                         "learned-surrogate study instead")
+    ap.add_argument("--surr-instances", type=int, default=625,
+                    help="surrogate study: media simulated for the training set")
+    ap.add_argument("--surr-snaps", type=int, default=33,
+                    help="surrogate study: snapshots per medium (pairs = snaps - 1)")
+    ap.add_argument("--surr-epochs", type=int, default=20)
+    ap.add_argument("--surr-batch", type=int, default=32)
+    ap.add_argument("--surr-eval", type=int, default=512, help="unseen media of the rollout")
+    ap.add_argument("--surr-steps", type=int, default=4096, help="time steps of the rollout")
     ap.add_argument("--time-steps", type=int, default=0,
                     help="override the workload's time steps per benchmark step (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.study == "surrogate":
+        return run_surrogate(args)
     if args.study:
         return run_study(args)
     if args.workload == "batched":

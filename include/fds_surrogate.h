@@ -6,8 +6,9 @@
  * reference (emtpb/pyfds) has no learned component: this library part serves the
  * parameter-sweep pattern built around Acoustic2D (pyfds/acoustics.py:89-128).
  *
- * Activations are bfloat16, channel-last ([batch][height][width][channels]), with
- * channels a multiple of 16. Convolutions run on the fifth-generation tensor
+ * Activations are bfloat16 in a channel-group blocked layout,
+ * [batch][channels / 8][height][width][8] (the 8 channels of a group are one 16-byte
+ * row per pixel), with channels a multiple of 16. Convolutions run on the fifth-generation tensor
  * cores (BF16 operands, FP32 accumulation in tensor memory); weights enter them
  * in a packed operand layout produced by fds_conv_pack / fds_adamw.
  *
@@ -42,14 +43,14 @@ typedef struct FdsConvArgs {
   int32_t dilation;             /* 1, 2, 4 or 8 */
   int32_t mode;                 /* FDS_CONV_* */
   int32_t reserved;
-  const void* x;      /* bf16 [B][H][W][cin] */
+  const void* x;      /* bf16 [B][cin/8][H][W][8] */
   const void* weight; /* bf16 packed operand, fds_conv_packed_elems(cin, cout) elements */
   const float* bias;  /* [cout] or NULL (forward modes) */
-  const void* resid;  /* bf16 [B][H][W][cout] or NULL */
-  const void* zin;    /* bf16 [B][H][W][cout]: pre-activation for gelu' (FDS_CONV_BWD_DATA) */
-  void* out_z;        /* bf16 [B][H][W][cout] or NULL */
-  void* out_h;        /* bf16 [B][H][W][cout] or NULL */
-  float* out_f32;     /* float32 [B][H][W][cout] (FDS_CONV_FWD_LINEAR) */
+  const void* resid;  /* bf16 [B][cout/8][H][W][8] or NULL */
+  const void* zin;    /* bf16 [B][cout/8][H][W][8]: pre-activation for gelu' (FDS_CONV_BWD_DATA) */
+  void* out_z;        /* bf16 [B][cout/8][H][W][8] or NULL */
+  void* out_h;        /* bf16 [B][cout/8][H][W][8] or NULL */
+  float* out_f32;     /* float32 [B][cout/8][H][W][8] (FDS_CONV_FWD_LINEAR) */
   int32_t* status;    /* device int32 or NULL */
 } FdsConvArgs;
 
@@ -67,8 +68,8 @@ int32_t fds_conv_pack(int32_t cin, int32_t cout, const float* w, void* wfwd, voi
 
 typedef struct FdsWgradArgs {
   int32_t batch, height, width, cin, cout, dilation; /* as in FdsConvArgs; height a multiple of 2 * dilation */
-  const void* x;     /* bf16 [B][H][W][cin]: the layer's input */
-  const void* dz;    /* bf16 [B][H][W][cout]: gradient at the layer's pre-activation */
+  const void* x;     /* bf16 [B][cin/8][H][W][8]: the layer's input */
+  const void* dz;    /* bf16 [B][cout/8][H][W][8]: gradient at the layer's pre-activation */
   float* partial;    /* [grid][9 * cout * cin + cout] float32: per-CTA weight and bias sums */
   int32_t grid;      /* CTAs (rows of `partial`); at most fds_conv_wgrad_max_grid() */
   int32_t reserved;
@@ -117,7 +118,7 @@ typedef struct FdsSurrData {
   const float* freq;    /* [instances] normalised source frequency */
   const float* zref;    /* [instances] impedance scale of the velocities */
   float* scale;         /* [count] energy norm of each input state */
-  void* x;              /* bf16 [count][H][W][16] network input */
+  void* x;              /* bf16 [count][2][H][W][8] network input (16 channels) */
   float* s;             /* float32 [count][H][W][4] normalised input state */
   float* t;             /* float32 [count][H][W][4] normalised target, or NULL */
 } FdsSurrData;
@@ -125,14 +126,14 @@ typedef struct FdsSurrData {
 /* scale, then x / s (and t when set). */
 int32_t fds_surr_pack(const FdsSurrData* d, void* stream);
 
-/* pred = s + y[..., :3]; writes dy = 2 (pred - t) / (count H W 3) as bf16
- * [count][H][W][16] (channels 3..15 zero) and per-CTA squared-error sums to
+/* pred = s + y[channels 0..2] (y float32 [count][2][H][W][8]); writes
+ * dy = 2 (pred - t) / (count H W 3) as bf16 [count][2][H][W][8] (channels 3..15 zero) and per-CTA squared-error sums to
  * `loss_parts` (fds_surr_loss_parts(count, H, W) floats). */
 int32_t fds_surr_loss(const FdsSurrData* d, const float* y, void* dy, float* loss_parts,
                       void* stream);
 int32_t fds_surr_loss_parts(int32_t count, int32_t height, int32_t width);
 
-/* state[inst][snap] = (s + y[..., :3]) de-normalised (the jump's result). */
+/* state[inst][snap] = (s + y[channels 0..2]) de-normalised (the jump's result). */
 int32_t fds_surr_unpack(const FdsSurrData* d, const float* y, void* stream);
 
 /* Per sample: sums of squared differences and of squares of the energy-weighted

@@ -2,6 +2,10 @@
 // the fifth-generation tensor cores, their weight gradients, a fused AdamW step,
 // and the packing of solver states into network inputs.
 //
+// Activations are stored channel-group blocked, [B][C/8][H][W][8] (bf16): the 8
+// channels of a pixel are one 16-byte row, and a row segment of one channel group
+// is contiguous in memory.
+//
 // Convolution (forward and data gradient), per CTA tile of kRows output rows x 128
 // pixels of one image:
 //   * TMA copies, per group of 8 input channels, kRows + 2 input rows of 128 + 2d
@@ -11,13 +15,13 @@
 //     K-major) of any tap (dy, dx) is the same slab pair at a start address moved
 //     by ((r + dy) * pitch + dx * d) * 16 bytes: no im2col copy.
 //   * The packed weights of the layer stay in shared memory for the whole kernel.
-//   * One thread issues 9 taps x cin/16 MMAs (M = 128, N = cout, K = 16) per output
-//     row into a tensor-memory accumulator; two accumulator sets and two staging
-//     buffers let the copies of the next tile and the epilogue of the previous one
-//     overlap the MMAs of the current one.
-//   * The epilogue (all 8 warps; warp w reads tensor-memory lanes 32 (w % 4) ..
-//     + 31, half of the columns) adds bias / residual, applies GELU or its
-//     derivative and stores bf16 (or float32).
+//   * Warp-specialised: a producer warp stages tiles, one thread of the MMA warp
+//     issues 9 taps x cin/16 MMAs (M = 128, N = cout, K = 16) per output row into
+//     a tensor-memory accumulator, 16 epilogue warps (one per tensor-memory lane
+//     quarter and output row) add bias / residual, apply GELU or its derivative
+//     and store bf16 (or float32). Two staging buffers and two accumulator sets
+//     let copies, MMAs and epilogues of consecutive tiles overlap; the roles hand
+//     off through mbarriers only.
 // Weight gradient: D[co][ci] (M = 64 >= cout, N = cin) summed over pixels per tap,
 // with both operands MN-major (channel-contiguous activations used as they are).
 //
@@ -36,7 +40,9 @@ namespace surr {
 constexpr int kTilePx = 128;   // pixels per tile row (M of the forward MMA)
 constexpr int kRows = 4;       // output rows per forward tile
 constexpr int kWRows = 2;      // output rows per weight-gradient tile
-constexpr int kThreads = 256;  // 8 warps
+constexpr int kConvThreads = 32 * (2 + 4 * kRows);  // producer, MMA, 16 epilogue warps
+constexpr int kBiasWarps = 8;                         // weight gradient: one pixel per thread
+constexpr int kWgradThreads = 32 * (2 + kBiasWarps);
 constexpr int kTmemCols = 512;
 constexpr int kAccStride = 64;  // tensor-memory columns per forward accumulator
 constexpr long long kWaitLimit = 1ll << 22;
@@ -113,8 +119,8 @@ __device__ __forceinline__ void issue_rows(const CUtensorMap* map, const Tile& t
                                            int row_shift, unsigned char* dst, uint64_t* bar) {
   for (int g = 0; g < ngroups; ++g)
     for (int k = 0; k < nrows; ++k)
-      tma_load_4d(dst + g * slab + k * pitch * 16, map, g * 8, tl.x0 - (rx - kTilePx) / 2,
-                  tl.y0 + (k - row_shift) * dil, tl.b, bar);
+      tma_load_4d(dst + g * slab + k * pitch * 16, map, 0, tl.x0 - (rx - kTilePx) / 2,
+                  tl.y0 + (k - row_shift) * dil, tl.b * ngroups + g, bar);
 }
 
 struct ConvDev {
@@ -130,66 +136,96 @@ struct ConvDev {
   int rx, pitch, slab, abuf, wbytes;
 };
 
-__device__ void conv_epilogue(const ConvDev& p, const Tile& tl, uint32_t tacc) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q = warp & 3, half = warp >> 2;
-  const int hc = p.cout / 2;
+// One output row of a tile (this warp's 32 pixels, every output channel) from its
+// tensor-memory accumulator: bias, GELU / residual or the GELU derivative, stores.
+__device__ void conv_epilogue_row(const ConvDev& p, const Tile& tl, int r, int q, uint32_t tacc) {
+  const int lane = threadIdx.x & 31;
   const int x = tl.x0 + 32 * q + lane;
-  for (int r = 0; r < kRows; ++r) {
-    const int y = tl.y0 + r * p.dil;
-    const size_t pix = ((size_t)tl.b * p.H + y) * p.W + x;
-    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 8) {
-      float v[8];
-      tmem_ld8(tacc + ((uint32_t)(32 * q) << 16) + r * kAccStride + c0, v);
-      const size_t o = pix * p.cout + c0;
-      if (p.mode == FDS_CONV_FWD_LINEAR) {
+  const size_t plane = (size_t)p.H * p.W;
+  const size_t pix = (size_t)(tl.y0 + r * p.dil) * p.W + x;
+  for (int c0 = 0; c0 < p.cout; c0 += 8) {
+    float v[8];
+    tmem_ld8(tacc + ((uint32_t)(32 * q) << 16) + (uint32_t)(r * kAccStride + c0), v);
+    // group c0 / 8 of the pixel: 8 consecutive values; the warp's 32 pixels are 512
+    // (bf16) or 1024 (float32) contiguous bytes
+    const size_t o = (((size_t)tl.b * (p.cout / 8) + (c0 >> 3)) * plane + pix) * 8;
+    if (p.mode == FDS_CONV_FWD_LINEAR) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
-        float4* dst = reinterpret_cast<float4*>(p.out_f32 + o);
-        dst[0] = make_float4(v[0], v[1], v[2], v[3]);
-        dst[1] = make_float4(v[4], v[5], v[6], v[7]);
-      } else if (p.mode == FDS_CONV_FWD_GELU) {
+      for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+      float4* dst = reinterpret_cast<float4*>(p.out_f32 + o);
+      dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+      dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+    } else if (p.mode == FDS_CONV_FWD_GELU) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
-        if (p.out_z) *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
-        float res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (p.resid) unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+      for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+      if (p.out_z) *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
+      float res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (p.resid) unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = gelu(v[i]) + res[i];
-        *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
-      } else {  // FDS_CONV_BWD_DATA
-        if (p.resid) {
-          float res[8];
-          unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+      for (int i = 0; i < 8; ++i) v[i] = gelu(v[i]) + res[i];
+      *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
+    } else {  // FDS_CONV_BWD_DATA
+      if (p.resid) {
+        float res[8];
+        unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] += res[i];
-        }
-        if (p.out_h) *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
-        float z[8];
-        unpack8(*reinterpret_cast<const uint4*>(p.zin + o), z);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] *= gelu_grad(z[i]);
-        *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
+        for (int i = 0; i < 8; ++i) v[i] += res[i];
       }
+      if (p.out_h) *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
+      float z[8];
+      unpack8(*reinterpret_cast<const uint4*>(p.zin + o), z);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] *= gelu_grad(z[i]);
+      *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
     }
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+// A bounded wait on an mbarrier phase that every lane of the warp takes together.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
+  const bool ok = mbar_wait(bar, parity, kWaitLimit);
+  return __all_sync(0xffffffffu, ok);
+}
+
+// Warp-uniform read of the CTA's abort flag.
+__device__ __forceinline__ bool aborted(volatile int* flag) {
+  return __shfl_sync(0xffffffffu, *flag, 0) != 0;
+}
+
+// Tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
+__device__ __forceinline__ int my_tiles(int ntiles) {
+  return blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+}
+
+// Warp roles: warp 0 stages tiles with TMA, warp 1 issues the MMAs, warps 2 ..
+// 2 + 4 kRows - 1 are the epilogue, warp w handling tensor-memory lane quarter
+// w % 4 (the quarter a warp may read) of output row (w - 2) / 4. Hand-offs are
+// mbarriers only: full[s] (copies landed) / empty[s] (the MMAs reading buffer s
+// completed), acc_full[a] (accumulator a complete) / acc_empty[a] (its 16
+// epilogue warps are done with it).
+__global__ void __launch_bounds__(kConvThreads, 1)
     conv3x3_kernel(const __grid_constant__ CUtensorMap xmap, const ConvDev p) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   unsigned char* abuf0 = sm + round_up(p.wbytes, 128);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(abuf0 + 2 * p.abuf);  // tma[2], mma[2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
-  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(abuf0 + 2 * p.abuf);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + 2;
+  uint64_t* acc_full = bars + 4;
+  uint64_t* acc_empty = bars + 6;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   if ((smem_addr(sm) & 127u) != 0) {  // TMA destinations need 128-byte alignment
     if (tid == 0 && p.status) atomicOr(p.status, FDS_SURR_STATUS_ALIGN);
     return;
   }
-
   if (tid == 0) {
-    for (int i = 0; i < 4; ++i) mbar_init(bars + i, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(full + i, 1);
+      mbar_init(empty + i, 1);
+      mbar_init(acc_full + i, 1);
+      mbar_init(acc_empty + i, 4 * kRows);
+    }
     *abort_flag = 0;
   }
   if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
@@ -204,46 +240,56 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tm = *tmem_slot;
-  const uint32_t w_addr = smem_addr(sm);
   const int grid = gridDim.x;
-  const int KC = p.cin / 16;
-  const uint32_t idesc = umma_idesc_bf16(128, p.cout);
-  const uint32_t tx_bytes = (uint32_t)((p.cin / 8) * (kRows + 2) * p.rx * 16);
+  const int nmine = my_tiles(p.ntiles);
 
-  // thread 0's bookkeeping of the copies and MMAs it issued per buffer
-  int tma_issued[2] = {0, 0}, tma_seen[2] = {0, 0};
-  int mma_issued[2] = {0, 0}, mma_seen[2] = {0, 0};
-
-  if (tid == 0) {
-    for (int s = 0; s < 2; ++s) {
-      const int t = blockIdx.x + s * grid;
-      if (t < p.ntiles) {
-        mbar_arrive_expect_tx(bars + s, tx_bytes);
-        issue_rows(&xmap, decode_tile(t, p.H, p.W, p.dil, kRows), p.dil, p.cin / 8, kRows + 2,
-                   p.rx, p.pitch, p.slab, 1, abuf0 + s * p.abuf, bars + s);
-        ++tma_issued[s];
+  if (warp == 0) {
+    // ---- producer
+    const uint32_t tx_bytes = (uint32_t)((p.cin / 8) * (kRows + 2) * p.rx * 16);
+    int issued[2] = {0, 0};
+    for (int k = 0; k < nmine; ++k) {
+      const int s = k & 1, u = k >> 1;
+      if (aborted(abort_flag)) break;
+      if (u > 0 && !warp_wait(empty + s, (uint32_t)((u - 1) & 1))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
       }
+      if (lane == 0) {
+        mbar_arrive_expect_tx(full + s, tx_bytes);
+        issue_rows(&xmap, decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kRows), p.dil,
+                   p.cin / 8, kRows + 2, p.rx, p.pitch, p.slab, 1, abuf0 + s * p.abuf, full + s);
+      }
+      __syncwarp();
+      ++issued[s];
     }
-  }
-  int k = 0;
-  Tile prev{0, 0, 0};
-  for (int t = blockIdx.x; t < p.ntiles; t += grid, ++k) {
-    const int s = k & 1;
-    if (tid == 0) {
-      if (!mbar_wait(bars + s, (uint32_t)((k >> 1) & 1), kWaitLimit)) {
-        *abort_flag = 1;
-      } else {
-        ++tma_seen[s];
-        tc_fence_after();
+    if (aborted(abort_flag))  // let copies in flight land before the memory goes away
+      for (int s = 0; s < 2; ++s)
+        if (issued[s] > 0) warp_wait(full + s, (uint32_t)((issued[s] - 1) & 1));
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    const int KC = p.cin / 16;
+    const uint32_t idesc = umma_idesc_bf16(128, p.cout);
+    const uint32_t w_addr = smem_addr(sm);
+    int last = -1;
+    for (int k = 0; k < nmine; ++k) {
+      const int s = k & 1, u = k >> 1;
+      if (aborted(abort_flag)) break;
+      if (!warp_wait(full + s, (uint32_t)(u & 1)) ||
+          (u > 0 && !warp_wait(acc_empty + s, (uint32_t)((u - 1) & 1)))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      if (lane == 0) {
         const uint32_t a0 = smem_addr(abuf0 + s * p.abuf);
         const uint32_t acc0 = tm + (uint32_t)(s * kRows * kAccStride);
         for (int r = 0; r < kRows; ++r) {
           uint32_t accumulate = 0;
           for (int tap = 0; tap < 9; ++tap) {
             const int dy = tap / 3, dx = tap % 3;
+            const uint32_t arow = a0 + (uint32_t)(((r + dy) * p.pitch + dx * p.dil) * 16);
             for (int kc = 0; kc < KC; ++kc) {
-              const uint32_t a =
-                  a0 + (uint32_t)(2 * kc * p.slab + ((r + dy) * p.pitch + dx * p.dil) * 16);
+              const uint32_t a = arow + (uint32_t)(2 * kc * p.slab);
               const uint32_t b = w_addr + (uint32_t)((tap * KC + kc) * p.cout * 32);
               umma_bf16(acc0 + r * kAccStride, umma_desc(a, (uint32_t)p.slab, 128u),
                         umma_desc(b, (uint32_t)(p.cout * 16), 128u), idesc, accumulate);
@@ -251,56 +297,36 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         }
-        umma_commit(bars + 2 + s);
-        ++mma_issued[s];
+        umma_commit(empty + s);
+        umma_commit(acc_full + s);
       }
+      __syncwarp();
+      last = k;
     }
-    if (k > 0) {
-      const int ps = s ^ 1;
-      const bool done = mbar_wait(bars + 2 + ps, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit);
-      if (!done) *abort_flag = 1;
-      tc_fence_after();
-      if (tid == 0 && done) {
-        ++mma_seen[ps];
-        // tile k-1's MMAs are complete: its staging buffer takes tile k+1
-        if (t + grid < p.ntiles && !*abort_flag) {
-          mbar_arrive_expect_tx(bars + ps, tx_bytes);
-          issue_rows(&xmap, decode_tile(t + grid, p.H, p.W, p.dil, kRows), p.dil, p.cin / 8,
-                     kRows + 2, p.rx, p.pitch, p.slab, 1, abuf0 + ps * p.abuf, bars + ps);
-          ++tma_issued[ps];
-        }
+    if (aborted(abort_flag) && last >= 0)  // MMAs complete in order: wait for the last
+      warp_wait(acc_full + (last & 1), (uint32_t)((last >> 1) & 1));
+  } else {
+    // ---- epilogue
+    const int q = warp & 3, r = (warp - 2) >> 2;
+    for (int k = 0; k < nmine; ++k) {
+      const int a = k & 1, u = k >> 1;
+      if (aborted(abort_flag)) break;
+      if (!warp_wait(acc_full + a, (uint32_t)(u & 1))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
       }
-      if (done) conv_epilogue(p, prev, tm + (uint32_t)(ps * kRows * kAccStride));
-    }
-    prev = decode_tile(t, p.H, p.W, p.dil, kRows);
-    tc_fence_before();
-    __syncthreads();
-    if (*abort_flag) break;
-  }
-  if (!*abort_flag && k > 0) {
-    const int ls = (k - 1) & 1;
-    if (mbar_wait(bars + 2 + ls, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit)) {
       tc_fence_after();
-      if (tid == 0) ++mma_seen[ls];
-      conv_epilogue(p, prev, tm + (uint32_t)(ls * kRows * kAccStride));
-    } else {
-      *abort_flag = 1;
+      conv_epilogue_row(p, decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kRows), r, q,
+                        tm + (uint32_t)(a * kRows * kAccStride));
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty + a);
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (*abort_flag && tid == 0) {
-    if (p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
-    // let every copy and MMA this CTA issued land before its memory goes away
-    for (int s = 0; s < 2; ++s) {
-      for (int u = tma_seen[s]; u < tma_issued[s]; ++u)
-        mbar_wait(bars + s, (uint32_t)(u & 1), kWaitLimit);
-      for (int u = mma_seen[s]; u < mma_issued[s]; ++u)
-        mbar_wait(bars + 2 + s, (uint32_t)(u & 1), kWaitLimit);
-    }
-  }
-  __syncthreads();
   tc_fence_after();
+  if (tid == 0 && *abort_flag && p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
   if (warp == 0) tmem_dealloc(tm, kTmemCols);
 }
 
@@ -313,22 +339,33 @@ struct WgradDev {
   int rx, pitch, xslab, dzslab, xbytes, buf;
 };
 
-__global__ void __launch_bounds__(kThreads, 1)
+// Warp roles: warp 0 stages tiles (input rows and gradient rows) with TMA, warp 1
+// issues the MMAs (every tile of the CTA accumulates into the same 9 per-tap
+// accumulators), warps 2..9 sum the bias gradient of each staged tile (thread =
+// pixel) and, at the end, read the accumulators out. A staging buffer is free once
+// its MMAs completed (commit) and the 8 bias warps arrived.
+__global__ void __launch_bounds__(kWgradThreads, 1)
     wgrad_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dzmap,
                  const WgradDev p) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * p.buf);  // tma[2], mma[2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
-  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * p.buf);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + 2;
+  uint64_t* done = bars + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   float* dbw = reinterpret_cast<float*>(tmem_slot + 4);  // [8 warps][64] bias partials
   if ((smem_addr(sm) & 127u) != 0) {  // TMA destinations need 128-byte alignment
     if (tid == 0 && p.status) atomicOr(p.status, FDS_SURR_STATUS_ALIGN);
     return;
   }
-
   if (tid == 0) {
-    for (int i = 0; i < 4; ++i) mbar_init(bars + i, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(full + i, 1);
+      mbar_init(empty + i, 1 + kBiasWarps);
+    }
+    mbar_init(done, 1);
     *abort_flag = 0;
   }
   if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
@@ -337,71 +374,78 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tm = *tmem_slot;
   const int grid = gridDim.x;
+  const int nmine = my_tiles(p.ntiles);
   const int KGx = p.cin / 8, KGz = p.cout / 8;
-  const uint32_t idesc = umma_idesc_bf16(64, p.cin) | kUmmaAMajorMN | kUmmaBMajorMN;
-  const uint32_t tx_bytes =
-      (uint32_t)(KGx * (kWRows + 2) * p.rx * 16 + KGz * kWRows * kTilePx * 16);
-  const size_t row_len = (size_t)9 * p.cout * p.cin + p.cout;
-  float* out = p.partial + (size_t)blockIdx.x * row_len;
-
   float db[48];
 #pragma unroll
   for (int i = 0; i < 48; ++i) db[i] = 0.0f;
 
-  int tma_issued[2] = {0, 0}, tma_seen[2] = {0, 0};
-  int mma_issued[2] = {0, 0}, mma_seen[2] = {0, 0};
-  auto issue = [&](int t, int s) {
-    const Tile tl = decode_tile(t, p.H, p.W, p.dil, kWRows);
-    unsigned char* base = sm + s * p.buf;
-    mbar_arrive_expect_tx(bars + s, tx_bytes);
-    issue_rows(&xmap, tl, p.dil, KGx, kWRows + 2, p.rx, p.pitch, p.xslab, 1, base, bars + s);
-    issue_rows(&dzmap, tl, p.dil, KGz, kWRows, kTilePx, kTilePx, p.dzslab, 0, base + p.xbytes,
-               bars + s);
-    ++tma_issued[s];
-  };
-  if (tid == 0) {
-    for (int s = 0; s < 2; ++s)
-      if (blockIdx.x + s * grid < p.ntiles) issue(blockIdx.x + s * grid, s);
-  }
-  int k = 0;
-  for (int t = blockIdx.x; t < p.ntiles; t += grid, ++k) {
-    const int s = k & 1;
-    const bool ready = mbar_wait(bars + s, (uint32_t)((k >> 1) & 1), kWaitLimit);
-    if (!ready) *abort_flag = 1;
-    if (tid == 0 && ready) {
-      ++tma_seen[s];
-      tc_fence_after();
-      const uint32_t xb = smem_addr(sm + s * p.buf);
-      const uint32_t zb = xb + (uint32_t)p.xbytes;
-      for (int r = 0; r < kWRows; ++r)
-        for (int w16 = 0; w16 < kTilePx / 16; ++w16) {
-          const uint32_t a = zb + (uint32_t)((r * kTilePx + w16 * 16) * 16);
-          const uint64_t ad = umma_desc(a, 128u, (uint32_t)p.dzslab);
-          for (int tap = 0; tap < 9; ++tap) {
-            const int dy = tap / 3, dx = tap % 3;
-            const uint32_t b =
-                xb + (uint32_t)(((r + dy) * p.pitch + w16 * 16 + dx * p.dil) * 16);
-            umma_bf16(tm + (uint32_t)(tap * p.cin), ad, umma_desc(b, 128u, (uint32_t)p.xslab),
-                      idesc, (k > 0 || r > 0 || w16 > 0) ? 1u : 0u);
-          }
-        }
-      umma_commit(bars + 2 + s);
-      ++mma_issued[s];
-      if (k > 0) {
-        // tile k-1's MMAs are complete (and its bias sums were read before the last
-        // barrier): its buffer takes tile k+1
-        const int ps = s ^ 1;
-        if (mbar_wait(bars + 2 + ps, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit)) {
-          ++mma_seen[ps];
-          if (t + grid < p.ntiles) issue(t + grid, ps);
-        } else {
-          *abort_flag = 1;
-        }
+  if (warp == 0) {
+    const uint32_t tx_bytes =
+        (uint32_t)(KGx * (kWRows + 2) * p.rx * 16 + KGz * kWRows * kTilePx * 16);
+    int issued[2] = {0, 0};
+    for (int k = 0; k < nmine; ++k) {
+      const int s = k & 1, u = k >> 1;
+      if (aborted(abort_flag)) break;
+      if (u > 0 && !warp_wait(empty + s, (uint32_t)((u - 1) & 1))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
       }
+      if (lane == 0) {
+        const Tile tl = decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kWRows);
+        unsigned char* base = sm + s * p.buf;
+        mbar_arrive_expect_tx(full + s, tx_bytes);
+        issue_rows(&xmap, tl, p.dil, KGx, kWRows + 2, p.rx, p.pitch, p.xslab, 1, base, full + s);
+        issue_rows(&dzmap, tl, p.dil, KGz, kWRows, kTilePx, kTilePx, p.dzslab, 0,
+                   base + p.xbytes, full + s);
+      }
+      __syncwarp();
+      ++issued[s];
     }
-    if (ready) {
-      // bias gradient: thread = one pixel of the tile, all cout channels
-      const unsigned char* zs = sm + s * p.buf + p.xbytes + tid * 16;
+    if (aborted(abort_flag))
+      for (int s = 0; s < 2; ++s)
+        if (issued[s] > 0) warp_wait(full + s, (uint32_t)((issued[s] - 1) & 1));
+  } else if (warp == 1) {
+    const uint32_t idesc = umma_idesc_bf16(64, p.cin) | kUmmaAMajorMN | kUmmaBMajorMN;
+    for (int k = 0; k < nmine; ++k) {
+      const int s = k & 1, u = k >> 1;
+      if (aborted(abort_flag) || !warp_wait(full + s, (uint32_t)(u & 1))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      if (lane == 0) {
+        const uint32_t xb = smem_addr(sm + s * p.buf);
+        const uint32_t zb = xb + (uint32_t)p.xbytes;
+        for (int r = 0; r < kWRows; ++r)
+          for (int w16 = 0; w16 < kTilePx / 16; ++w16) {
+            const uint32_t a = zb + (uint32_t)((r * kTilePx + w16 * 16) * 16);
+            const uint64_t ad = umma_desc(a, 128u, (uint32_t)p.dzslab);
+            for (int tap = 0; tap < 9; ++tap) {
+              const int dy = tap / 3, dx = tap % 3;
+              const uint32_t b =
+                  xb + (uint32_t)(((r + dy) * p.pitch + w16 * 16 + dx * p.dil) * 16);
+              umma_bf16(tm + (uint32_t)(tap * p.cin), ad, umma_desc(b, 128u, (uint32_t)p.xslab),
+                        idesc, (k > 0 || r > 0 || w16 > 0) ? 1u : 0u);
+            }
+          }
+        umma_commit(empty + s);
+      }
+      __syncwarp();
+    }
+    // completion of every MMA of this CTA (also when there were none, or on abort)
+    if (lane == 0) umma_commit(done);
+    __syncwarp();
+  } else {
+    const int px = tid - 64;  // pixel of the tile: row px / 128, column px % 128
+    for (int k = 0; k < nmine; ++k) {
+      const int s = k & 1, u = k >> 1;
+      if (aborted(abort_flag)) break;
+      if (!warp_wait(full + s, (uint32_t)(u & 1))) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      const unsigned char* zs = sm + s * p.buf + p.xbytes + px * 16;
       for (int g = 0; g < KGz; ++g) {
         float f[8];
         unpack8(*reinterpret_cast<const uint4*>(zs + g * p.dzslab), f);
@@ -411,32 +455,24 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int gg = 0; gg < 6; ++gg)
             if (gg == g) db[gg * 8 + i] += f[i];
       }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty + s);
     }
-    tc_fence_before();
-    __syncthreads();
-    if (*abort_flag) break;
   }
-  // the last tile's MMAs (the one before it was waited inside the loop)
-  if (tid == 0 && !*abort_flag && k > 0) {
-    const int ls = (k - 1) & 1;
-    if (mbar_wait(bars + 2 + ls, (uint32_t)(((k - 1) >> 1) & 1), kWaitLimit))
-      ++mma_seen[ls];
-    else
-      *abort_flag = 1;
-  }
-  tc_fence_before();
   __syncthreads();
+  const bool ok = !*abort_flag && warp_wait(done, 0u);
   tc_fence_after();
-  const bool failed = *abort_flag != 0;
-  if (!failed) {
+  if (ok && warp >= 2) {
     // D row m (output channel) sits in lane 32 (m / 16) + m % 16
-    const int q = warp & 3, half = warp >> 2;
+    const int q = warp & 3, half = (warp - 2) >> 2;
     const int m = 16 * q + lane;
     const int hc = p.cin / 2;
+    const size_t row_len = (size_t)9 * p.cout * p.cin + p.cout;
+    float* out = p.partial + (size_t)blockIdx.x * row_len;
     for (int tap = 0; tap < 9; ++tap)
       for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 8) {
         float v[8];
-        if (k > 0) {
+        if (nmine > 0) {
           tmem_ld8(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(tap * p.cin + c0), v);
         } else {
 #pragma unroll
@@ -454,23 +490,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       float v = db[i];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) dbw[warp * 64 + i] = v;
-    }
-    __syncthreads();
-    if (tid < p.cout) {
-      float v = 0.0f;
-      for (int w = 0; w < kThreads / 32; ++w) v += dbw[w * 64 + tid];
-      out[(size_t)9 * p.cout * p.cin + tid] = v;
-    }
-  } else if (tid == 0) {
-    if (p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
-    for (int s = 0; s < 2; ++s) {
-      for (int u = tma_seen[s]; u < tma_issued[s]; ++u)
-        mbar_wait(bars + s, (uint32_t)(u & 1), kWaitLimit);
-      for (int u = mma_seen[s]; u < mma_issued[s]; ++u)
-        mbar_wait(bars + 2 + s, (uint32_t)(u & 1), kWaitLimit);
+      if (lane == 0) dbw[(warp - 2) * 64 + i] = v;
     }
   }
+  __syncthreads();
+  if (ok && tid < p.cout) {
+    float v = 0.0f;
+    for (int w = 0; w < kBiasWarps; ++w) v += dbw[w * 64 + tid];
+    p.partial[(size_t)blockIdx.x * ((size_t)9 * p.cout * p.cin + p.cout) +
+              (size_t)9 * p.cout * p.cin + tid] = v;
+  }
+  if (tid == 0 && !ok && p.status) atomicOr(p.status, FDS_SURR_STATUS_TIMEOUT);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -576,9 +606,9 @@ __global__ void __launch_bounds__(256) pack_input_kernel(const FdsSurrData d) {
   const float sp = (float)st[i] * inv, svx = z * (float)st[plane + i] * inv,
               svy = z * (float)st[2 * plane + i] * inv;
   float f[8] = {md[i], md[plane + i], sp, svx, svy, d.freq[inst], 0.0f, 0.0f};
-  uint4* x = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(d.x) + ((size_t)k * plane + i) * 16);
-  x[0] = pack8(f);
-  x[1] = make_uint4(0u, 0u, 0u, 0u);
+  uint4* x = reinterpret_cast<uint4*>(d.x);  // [count][2][plane] rows of 8 channels
+  x[(size_t)k * 2 * plane + i] = pack8(f);
+  x[((size_t)k * 2 + 1) * plane + i] = make_uint4(0u, 0u, 0u, 0u);
   reinterpret_cast<float4*>(d.s)[(size_t)k * plane + i] = make_float4(sp, svx, svy, 0.0f);
   if (d.t) {
     const T* tg = state_at<T>(d, k, 1);
@@ -596,15 +626,18 @@ __global__ void __launch_bounds__(256)
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   float err = 0.0f;
   if (i < n) {
-    const float4 o = reinterpret_cast<const float4*>(y)[i * 4];
+    const size_t plane = (size_t)d.height * d.width;
+    const size_t k = i / plane, pix = i % plane;
+    // y: float32 [count][2][plane][8]; the state channels are group 0, values 0..2
+    const float4 o = reinterpret_cast<const float4*>(y)[(k * 2 * plane + pix) * 2];
     const float4 s = reinterpret_cast<const float4*>(d.s)[i];
     const float4 t = reinterpret_cast<const float4*>(d.t)[i];
     const float e0 = s.x + o.x - t.x, e1 = s.y + o.y - t.y, e2 = s.z + o.z - t.z;
     err = e0 * e0 + e1 * e1 + e2 * e2;
     float f[8] = {gscale * e0, gscale * e1, gscale * e2, 0, 0, 0, 0, 0};
-    uint4* g = reinterpret_cast<uint4*>(dy + i * 16);
-    g[0] = pack8(f);
-    g[1] = make_uint4(0u, 0u, 0u, 0u);
+    uint4* g = reinterpret_cast<uint4*>(dy);
+    g[k * 2 * plane + pix] = pack8(f);
+    g[(k * 2 + 1) * plane + pix] = make_uint4(0u, 0u, 0u, 0u);
   }
   const float s = block_sum(err, red);
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
@@ -619,7 +652,7 @@ __global__ void __launch_bounds__(256) unpack_kernel(const FdsSurrData d, const 
   const int inst = d.inst[k];
   const float sc = d.scale[k];
   const float z = d.zref[inst];
-  const float4 o = reinterpret_cast<const float4*>(y)[((size_t)k * plane + i) * 4];
+  const float4 o = reinterpret_cast<const float4*>(y)[((size_t)k * 2 * plane + i) * 2];
   const float4 s = reinterpret_cast<const float4*>(d.s)[(size_t)k * plane + i];
   T* st = const_cast<T*>(state_at<T>(d, k, 0));
   float pv = (s.x + o.x) * sc;
@@ -674,13 +707,13 @@ int sm_count() {
   return n;
 }
 
-// [B][H][W][C] bf16 activations; boxes of 8 channels x bw pixels x 1 row.
+// [B][C/8][H][W][8] bf16 activations as a 4-D tensor (8, W, H, B * C/8); boxes of
+// 8 channels x bw pixels x 1 row x 1 group.
 bool encode_act_map(CUtensorMap* m, const void* base, int B, int H, int W, int C, int bw) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc || !base || ((uintptr_t)base & 15) != 0 || bw > 256) return false;
-  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
-  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2,
-                                 (cuuint64_t)H * W * C * 2};
+  const cuuint64_t dims[4] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B * (C / 8)};
+  const cuuint64_t strides[3] = {16, (cuuint64_t)W * 16, (cuuint64_t)H * W * 16};
   const cuuint32_t box[4] = {8, (cuuint32_t)bw, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box,
@@ -780,7 +813,7 @@ extern "C" int32_t fds_conv3x3(const FdsConvArgs* a, void* stream) {
   int32_t rc = set_smem(reinterpret_cast<const void*>(conv3x3_kernel), smem);
   if (rc != FDS_OK) return rc;
   const int grid = p.ntiles < sm_count() ? p.ntiles : sm_count();
-  conv3x3_kernel<<<grid, kThreads, smem > kMinSmem ? smem : kMinSmem,
+  conv3x3_kernel<<<grid, kConvThreads, smem > kMinSmem ? smem : kMinSmem,
                    static_cast<cudaStream_t>(stream)>>>(map, p);
   return launch_error("conv3x3_kernel");
 }
@@ -819,7 +852,7 @@ extern "C" int32_t fds_conv3x3_wgrad(const FdsWgradArgs* a, void* stream) {
   p.xbytes = (a->cin / 8) * p.xslab;
   // the M = 64 operand spans 8 channel groups; the ones past cout are never used
   p.buf = p.xbytes + 8 * p.dzslab;
-  const int smem = 2 * p.buf + 64 + 8 * 64 * 4;
+  const int smem = 2 * p.buf + 64 + kBiasWarps * 64 * 4;
   if (smem > kMaxSmem)
     return set_error(FDS_E_SIZE, "weight gradient %d->%d dilation %d needs %d bytes of shared memory",
                      a->cin, a->cout, a->dilation, smem);
@@ -829,7 +862,7 @@ extern "C" int32_t fds_conv3x3_wgrad(const FdsWgradArgs* a, void* stream) {
     return set_error(FDS_E_LAUNCH, "tensor map encoding failed for the weight gradient");
   int32_t rc = set_smem(reinterpret_cast<const void*>(wgrad_kernel), smem);
   if (rc != FDS_OK) return rc;
-  wgrad_kernel<<<a->grid, kThreads, smem > kMinSmem ? smem : kMinSmem,
+  wgrad_kernel<<<a->grid, kWgradThreads, smem > kMinSmem ? smem : kMinSmem,
                  static_cast<cudaStream_t>(stream)>>>(xm, zm, p);
   return launch_error("wgrad_kernel");
 }

@@ -18,7 +18,8 @@ Every network operation runs in libfdsgpu.so (include/fds_surrogate.h): the
 convolutions, their data and weight gradients on the tensor cores (tcgen05, BF16
 operands, FP32 accumulation), the fused AdamW step, and the packing of states.
 PyTorch only owns the device memory. There is no CPU path: the library must be
-built and a GPU present.
+built and a GPU present. Activations are bf16 in the channel-group blocked layout
+[batch][channels/8][height][width][8] of include/fds_surrogate.h.
 
 Network (``DEFAULT_LAYERS``): 8 convolution layers, 48 channels, GELU (tanh form),
 residual connections on layers 1..6, dilations 1, 2, 4, 8, 8, 4, 2, 1 so that the
@@ -123,21 +124,27 @@ class ConvNet:
         hw = (batch, height, width)
         nl = len(self.layers)
         c = lambda l: self.layers[l][1]
-        b = {"x": torch.zeros(hw + (IN_CH,), dtype=bf, device=dev),
+        cmax = max(max(l[0], l[1]) for l in self.layers)
+
+        def act(ch, dtype=bf, zero=False):  # [batch][ch/8][height][width][8]
+            f = torch.zeros if zero else torch.empty
+            return f((batch, ch // 8, height, width, 8), dtype=dtype, device=dev)
+
+        b = {"x": act(IN_CH, zero=True),
              "s": torch.zeros(hw + (4,), dtype=f32, device=dev),
              "t": torch.zeros(hw + (4,), dtype=f32, device=dev) if train else None,
              "scale": torch.zeros(batch, dtype=f32, device=dev),
-             "y": torch.zeros(hw + (OUT_CH,), dtype=f32, device=dev)}
+             "y": act(OUT_CH, f32, zero=True)}
         if train:
-            b["z"] = [torch.empty(hw + (c(l),), dtype=bf, device=dev) for l in range(nl - 1)]
-            b["h"] = [torch.empty(hw + (c(l),), dtype=bf, device=dev) for l in range(nl - 1)]
-            b["dy"] = torch.empty(hw + (OUT_CH,), dtype=bf, device=dev)
-            b["dz"] = [torch.empty(hw + (48,), dtype=bf, device=dev) for _ in range(2)]
-            b["dh"] = [torch.empty(hw + (48,), dtype=bf, device=dev) for _ in range(2)]
+            b["z"] = [act(c(l)) for l in range(nl - 1)]
+            b["h"] = [act(c(l)) for l in range(nl - 1)]
+            b["dy"] = act(OUT_CH)
+            b["dz"] = [act(cmax) for _ in range(2)]
+            b["dh"] = [act(cmax) for _ in range(2)]
             nparts = self.lib.fds_surr_loss_parts(batch, height, width)
             b["loss_parts"] = torch.zeros(nparts, dtype=f32, device=dev)
         else:
-            b["h"] = [torch.empty(hw + (48,), dtype=bf, device=dev) for _ in range(2)]
+            b["h"] = [act(cmax) for _ in range(2)]
         self._bufs[key] = b
         return b
 
@@ -443,11 +450,11 @@ def _rollout_setup(fields, n, torch, dev):
     init = S.clone()
     r_src = BatchRunner(fields, T_SRC)
     r_src.capture()
+    # every later runner (this one, and the fallback runners of a rollout) is
+    # planned at step T_SRC, where the source signal is zero: the fields stay there
     for f in fields:
         f.step = T_SRC
     r = _fd_runner(fields)
-    for f in fields:
-        f.step = 0
     S.copy_(init)
     return S, r_src, r
 

@@ -45,6 +45,17 @@ def _bf16(rng, shape, scale=1.0):
     return torch.tensor(rng.standard_normal(shape) * scale, dtype=torch.float32).to(torch.bfloat16)
 
 
+def _blk(t):
+    """[B][H][W][C] -> the kernels' blocked layout [B][C/8][H][W][8]."""
+    B, H, W, C = t.shape
+    return t.reshape(B, H, W, C // 8, 8).permute(0, 3, 1, 2, 4).contiguous()
+
+
+def _unblk(t):
+    B, G, H, W, _ = t.shape
+    return t.permute(0, 2, 3, 1, 4).reshape(B, H, W, G * 8)
+
+
 def _packed(env, w):
     cout, cin = w.shape[1], w.shape[2]
     wt = torch.tensor(w, dtype=torch.float32, device=env["dev"])
@@ -59,7 +70,7 @@ def _conv(env, x, weight, cin, cout, dil, mode, bias=None, resid=None, zin=None,
     capi = env["capi"]
     status = torch.zeros(1, dtype=torch.int32, device=env["dev"])
     a = capi.FdsConvArgs()
-    a.batch, a.height, a.width = x.shape[0], x.shape[1], x.shape[2]
+    a.batch, a.height, a.width = x.shape[0], x.shape[2], x.shape[3]
     a.cin, a.cout, a.dilation, a.mode = cin, cout, dil, mode
     a.x, a.weight, a.bias, a.resid, a.zin = _p(x), _p(weight), _p(bias), _p(resid), _p(zin)
     a.out_z, a.out_h, a.out_f32, a.status = _p(out_z), _p(out_h), _p(out_f32), _p(status)
@@ -74,7 +85,7 @@ def _wgrad(env, x, dz, cin, cout, dil, grid):
     n = 9 * cout * cin + cout
     part = torch.full((grid, n), float("nan"), dtype=torch.float32, device=env["dev"])
     a = capi.FdsWgradArgs()
-    a.batch, a.height, a.width = x.shape[0], x.shape[1], x.shape[2]
+    a.batch, a.height, a.width = x.shape[0], x.shape[2], x.shape[3]
     a.cin, a.cout, a.dilation = cin, cout, dil
     a.x, a.dz, a.partial, a.grid, a.status = _p(x), _p(dz), _p(part), grid, _p(status)
     capi.check(env["lib"].fds_conv3x3_wgrad(C.byref(a), _stream()))
@@ -113,19 +124,19 @@ def test_probe_conv_single_tile(env):
     w = rng.standard_normal((9, 16, 16)) * 0.2
     b = rng.standard_normal(16) * 0.1
     wf, _ = _packed(env, w)
-    out = torch.full((1, 4, 128, 16), float("nan"), dtype=torch.float32, device=env["dev"])
+    out = torch.full((1, 2, 4, 128, 8), float("nan"), dtype=torch.float32, device=env["dev"])
     bias = torch.tensor(b, dtype=torch.float32, device=env["dev"])
-    _conv(env, x.to(env["dev"]), wf, 16, 16, 1, env["capi"].CONV_FWD_LINEAR, bias=bias,
+    _conv(env, _blk(x).to(env["dev"]), wf, 16, 16, 1, env["capi"].CONV_FWD_LINEAR, bias=bias,
           out_f32=out)
     ref = _oracle_conv(x, w, b, 1)
-    assert _rel(out.cpu().numpy(), ref) < 1e-4
+    assert _rel(_unblk(out).cpu().numpy(), ref) < 1e-4
 
 
 def test_probe_wgrad_single_tile(env):
     rng = np.random.default_rng(2)
     x = _bf16(rng, (1, 2, 128, 16))
     dz = _bf16(rng, (1, 2, 128, 16))
-    dw, db = _wgrad(env, x.to(env["dev"]), dz.to(env["dev"]), 16, 16, 1, grid=1)
+    dw, db = _wgrad(env, _blk(x).to(env["dev"]), _blk(dz).to(env["dev"]), 16, 16, 1, grid=1)
     rw, rb = _oracle_wgrad(x, dz, 16, 16, 1)
     assert _rel(dw, rw) < 1e-4
     assert _rel(db, rb) < 1e-4
@@ -142,10 +153,11 @@ def test_conv_linear(env, cin, cout, dil):
     w = rng.standard_normal((9, cout, cin)) / np.sqrt(9 * cin)
     b = rng.standard_normal(cout) * 0.1
     wf, _ = _packed(env, w)
-    out = torch.full((B, H, W, cout), float("nan"), dtype=torch.float32, device=env["dev"])
-    _conv(env, x.to(env["dev"]), wf, cin, cout, dil, env["capi"].CONV_FWD_LINEAR,
+    out = torch.full((B, cout // 8, H, W, 8), float("nan"), dtype=torch.float32,
+                     device=env["dev"])
+    _conv(env, _blk(x).to(env["dev"]), wf, cin, cout, dil, env["capi"].CONV_FWD_LINEAR,
           bias=torch.tensor(b, dtype=torch.float32, device=env["dev"]), out_f32=out)
-    assert _rel(out.cpu().numpy(), _oracle_conv(x, w, b, dil)) < 1e-4
+    assert _rel(_unblk(out).cpu().numpy(), _oracle_conv(x, w, b, dil)) < 1e-4
 
 
 @pytest.mark.parametrize("residual", [False, True])
@@ -156,16 +168,16 @@ def test_conv_gelu(env, residual):
     w = rng.standard_normal((9, c, c)) / np.sqrt(9 * c)
     b = rng.standard_normal(c) * 0.1
     wf, _ = _packed(env, w)
-    z = torch.empty((B, H, W, c), dtype=torch.bfloat16, device=env["dev"])
+    z = torch.empty((B, c // 8, H, W, 8), dtype=torch.bfloat16, device=env["dev"])
     h = torch.empty_like(z)
-    xd = x.to(env["dev"])
+    xd = _blk(x).to(env["dev"])
     _conv(env, xd, wf, c, c, dil, env["capi"].CONV_FWD_GELU,
           bias=torch.tensor(b, dtype=torch.float32, device=env["dev"]),
           resid=xd if residual else None, out_z=z, out_h=h)
     zr = _oracle_conv(x, w, b, dil)
     hr = so.gelu(torch.tensor(zr)).numpy() + (x.float().numpy() if residual else 0.0)
-    assert _rel(z.float().cpu().numpy(), zr) < 1e-2
-    assert _rel(h.float().cpu().numpy(), hr) < 1e-2
+    assert _rel(_unblk(z).float().cpu().numpy(), zr) < 1e-2
+    assert _rel(_unblk(h).float().cpu().numpy(), hr) < 1e-2
 
 
 @pytest.mark.parametrize("cin,cout,dil,residual", [(48, 48, 8, True), (48, 16, 1, False),
@@ -180,11 +192,11 @@ def test_conv_backward_data(env, cin, cout, dil, residual):
     res = _bf16(rng, (B, H, W, cin))
     w = rng.standard_normal((9, cout, cin)) / np.sqrt(9 * cin)
     _, wb = _packed(env, w)
-    dz = torch.empty((B, H, W, cin), dtype=torch.bfloat16, device=env["dev"])
+    dz = torch.empty((B, cin // 8, H, W, 8), dtype=torch.bfloat16, device=env["dev"])
     dh = torch.empty_like(dz)
-    _conv(env, g.to(env["dev"]), wb, cout, cin, dil, env["capi"].CONV_BWD_DATA,
-          resid=res.to(env["dev"]) if residual else None, zin=zin.to(env["dev"]), out_z=dz,
-          out_h=dh)
+    _conv(env, _blk(g).to(env["dev"]), wb, cout, cin, dil, env["capi"].CONV_BWD_DATA,
+          resid=_blk(res).to(env["dev"]) if residual else None, zin=_blk(zin).to(env["dev"]),
+          out_z=dz, out_h=dh)
     # oracle: data gradient of y = conv(x, w) contracted with g
     xt = torch.zeros((B, H, W, cin), dtype=torch.float64, requires_grad=True)
     wt = torch.tensor(w, dtype=torch.float32).to(torch.bfloat16).to(torch.float64)
@@ -192,8 +204,8 @@ def test_conv_backward_data(env, cin, cout, dil, residual):
     gr = xt.grad.numpy() + (res.float().numpy() if residual else 0.0)
     zt = torch.tensor(zin.float().numpy(), dtype=torch.float64, requires_grad=True)
     so.gelu(zt).sum().backward()
-    assert _rel(dh.float().cpu().numpy(), gr) < 1e-2
-    assert _rel(dz.float().cpu().numpy(), gr * zt.grad.numpy()) < 1e-2
+    assert _rel(_unblk(dh).float().cpu().numpy(), gr) < 1e-2
+    assert _rel(_unblk(dz).float().cpu().numpy(), gr * zt.grad.numpy()) < 1e-2
 
 
 @pytest.mark.parametrize("cin,cout,dil", [(48, 48, 8), (16, 48, 1), (48, 16, 2)])
@@ -203,7 +215,7 @@ def test_wgrad(env, cin, cout, dil):
     x = _bf16(rng, (B, H, W, cin))
     dz = _bf16(rng, (B, H, W, cout))
     grid = env["lib"].fds_conv_wgrad_max_grid()
-    dw, db = _wgrad(env, x.to(env["dev"]), dz.to(env["dev"]), cin, cout, dil, grid)
+    dw, db = _wgrad(env, _blk(x).to(env["dev"]), _blk(dz).to(env["dev"]), cin, cout, dil, grid)
     rw, rb = _oracle_wgrad(x, dz, cin, cout, dil)
     assert _rel(dw, rw) < 1e-4
     assert _rel(db, rb) < 1e-4
@@ -264,10 +276,10 @@ def test_pack_and_unpack(env):
     for k, i in enumerate((2, 0)):
         x, s, sc = so.pack_inputs(state[i, 0], media[i], freq[i], zref[i])
         assert abs(float(b["scale"][k]) - sc) < 1e-5 * sc
-        assert _rel(b["x"][k].float().cpu().numpy(), x) < 1e-2
+        assert _rel(_unblk(b["x"][k:k + 1])[0].float().cpu().numpy(), x) < 1e-2
         assert _rel(b["s"][k].cpu().numpy(), s) < 1e-5
     y = torch.tensor(rng.standard_normal((2, n, n, 16)) * 0.01, dtype=torch.float32, device=dev)
-    b["y"].copy_(y)
+    b["y"].copy_(_blk(y))
     capi.check(lib.fds_surr_unpack(C.byref(d), _p(b["y"]), _stream()))
     torch.cuda.synchronize()
     out = S.cpu().numpy()
@@ -300,7 +312,7 @@ def test_network_gradients_match_oracle(env):
     s = rng.standard_normal((B, n, W, 4)).astype(np.float32)
     t = (s + rng.standard_normal((B, n, W, 4)) * 0.3).astype(np.float32)
     s[..., 3] = t[..., 3] = 0
-    b["x"].copy_(x.to(env["dev"]))
+    b["x"].copy_(_blk(x).to(env["dev"]))
     b["s"].copy_(torch.tensor(s))
     b["t"].copy_(torch.tensor(t))
     shape = (B, n, W)
@@ -323,3 +335,52 @@ def test_network_gradients_match_oracle(env):
     for k, ((gw, gb), (rw, rb)) in enumerate(zip(grads, ref)):
         assert _rel(gw, rw) < 3e-2, ("layer", k, _rel(gw, rw))
         assert _rel(gb, rb) < 3e-2, ("layer bias", k, _rel(gb, rb))
+
+
+# ------------------------------------------------------------------ pipeline
+
+@pytest.fixture(scope="module")
+def small_specs(env):
+    from pyfds_gb300 import workloads
+    return workloads.surrogate_media(4, seed=123, n=128, nt=env["surr"].T_SRC + 4 * 64)
+
+
+def test_rollout_with_rejected_checks_is_the_solver(env, small_specs):
+    """tol = 0: the first check rejects every instance, the solver takes over, and
+    the result is the plain FP64 rollout bit for bit."""
+    surr = env["surr"]
+    steps = surr.T_SRC + 4 * 64
+    ref, _ = surr.fd_rollout(small_specs, steps)
+    net = surr.ConvNet(seed=1)
+    out, _, rep = surr.surrogate_rollout(net, small_specs, steps, check_every=8, tol=0.0)
+    assert rep["fallback_instances"] == len(small_specs)
+    assert rep["network_jumps"] == len(small_specs)  # the check jump only
+    assert torch.equal(out, ref)
+
+
+def test_rollout_with_accepted_checks_uses_the_network(env, small_specs):
+    surr = env["surr"]
+    steps = surr.T_SRC + 4 * 64
+    net = surr.ConvNet(seed=1)
+    out, _, rep = surr.surrogate_rollout(net, small_specs, steps, check_every=2, tol=1e30)
+    assert rep["fallback_instances"] == 0
+    # jumps 0 and 2 are checks (network + solver), 1 and 3 network jumps
+    assert rep["network_jumps"] == 4 * len(small_specs)
+    assert rep["solver_windows"] == 2 * len(small_specs)
+    assert len(rep["checks"]) == 2
+    assert torch.isfinite(out).all()
+
+
+def test_training_reduces_the_jump_error(env):
+    """A short training run on solver snapshots: the loss (mean squared error of the
+    normalised jump) falls well below its starting value, which is the error of
+    leaving the state unchanged (the untrained output is near zero)."""
+    surr = env["surr"]
+    data = surr.generate_data(8, 5, seed=7, n=128)
+    assert data.state.shape == (8, 5, 3, 128, 128)
+    assert torch.isfinite(data.state).all()
+    net = surr.ConvNet(seed=2)
+    losses, _ = surr.train(net, data, epochs=25, batch=8, lr=2e-3, seed=0, log_every=1)
+    first = np.mean([l for _, l in losses[:3]])
+    last = np.mean([l for _, l in losses[-3:]])
+    assert last < 0.5 * first, (first, last)
