@@ -112,14 +112,16 @@ __device__ __forceinline__ Tile decode_tile(int t, int H, int W, int dil, int ro
   return {t / nyb, yb * rows * dil + j, xq * kTilePx};
 }
 
-// Stages `nrows` input rows (spaced dil, the first one row above output row 0)
-// of `ngroups` 8-channel groups into slabs `slab` bytes apart.
+// Stages `nrows` rows (spaced dil, starting row_shift rows above output row 0) of
+// `ngroups` 8-channel groups, rx pixels each; row k of group g lands at
+// dst + g * gstride + k * rstride.
 __device__ __forceinline__ void issue_rows(const CUtensorMap* map, const Tile& tl, int dil,
-                                           int ngroups, int nrows, int rx, int pitch, int slab,
-                                           int row_shift, unsigned char* dst, uint64_t* bar) {
+                                           int ngroups, int nrows, int rx, int gstride,
+                                           int rstride, int row_shift, unsigned char* dst,
+                                           uint64_t* bar) {
   for (int g = 0; g < ngroups; ++g)
     for (int k = 0; k < nrows; ++k)
-      tma_load_4d(dst + g * slab + k * pitch * 16, map, 0, tl.x0 - (rx - kTilePx) / 2,
+      tma_load_4d(dst + g * gstride + k * rstride, map, 0, tl.x0 - (rx - kTilePx) / 2,
                   tl.y0 + (k - row_shift) * dil, tl.b * ngroups + g, bar);
 }
 
@@ -136,43 +138,49 @@ struct ConvDev {
   int rx, pitch, slab, abuf, wbytes;
 };
 
-// One output row of a tile (this warp's 32 pixels, every output channel) from its
-// tensor-memory accumulator: bias, GELU / residual or the GELU derivative, stores.
-__device__ void conv_epilogue_row(const ConvDev& p, const Tile& tl, int r, int q, uint32_t tacc) {
-  const int lane = threadIdx.x & 31;
-  const int x = tl.x0 + 32 * q + lane;
-  const size_t plane = (size_t)p.H * p.W;
-  const size_t pix = (size_t)(tl.y0 + r * p.dil) * p.W + x;
-  for (int c0 = 0; c0 < p.cout; c0 += 8) {
+// One output row of a tile (this warp's 32 pixels, all NG * 8 output channels)
+// from its tensor-memory accumulator: bias, GELU / residual or the GELU
+// derivative, stores. `res` is the residual row, loaded before the accumulator
+// was ready.
+template <int NG>
+__device__ __forceinline__ void conv_epilogue_row(const ConvDev& p, size_t o0, size_t gstride,
+                                                  uint32_t tacc, const float* bias_s,
+                                                  const uint4 (&res)[NG]) {
+  uint32_t acc[NG / 2][16];
+#pragma unroll
+  for (int j = 0; j < NG / 2; ++j) tmem_ld16_async(tacc + 16 * j, acc[j]);
+  tmem_ld_wait();
+#pragma unroll
+  for (int j = 0; j < NG / 2; ++j) tmem_reg_fence(acc[j]);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
     float v[8];
-    tmem_ld8(tacc + ((uint32_t)(32 * q) << 16) + (uint32_t)(r * kAccStride + c0), v);
-    // group c0 / 8 of the pixel: 8 consecutive values; the warp's 32 pixels are 512
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(acc[g / 2][(g & 1) * 8 + i]);
+    // group g of the pixel: 8 consecutive values; the warp's 32 pixels are 512
     // (bf16) or 1024 (float32) contiguous bytes
-    const size_t o = (((size_t)tl.b * (p.cout / 8) + (c0 >> 3)) * plane + pix) * 8;
+    const size_t o = o0 + g * gstride;
     if (p.mode == FDS_CONV_FWD_LINEAR) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+      for (int i = 0; i < 8; ++i) v[i] += bias_s[g * 8 + i];
       float4* dst = reinterpret_cast<float4*>(p.out_f32 + o);
       dst[0] = make_float4(v[0], v[1], v[2], v[3]);
       dst[1] = make_float4(v[4], v[5], v[6], v[7]);
     } else if (p.mode == FDS_CONV_FWD_GELU) {
 #pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] += p.bias ? p.bias[c0 + i] : 0.0f;
+      for (int i = 0; i < 8; ++i) v[i] += bias_s[g * 8 + i];
       if (p.out_z) *reinterpret_cast<uint4*>(p.out_z + o) = pack8(v);
-      float res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (p.resid) unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+      float rr[8];
+      unpack8(res[g], rr);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) v[i] = gelu(v[i]) + res[i];
+      for (int i = 0; i < 8; ++i) v[i] = gelu(v[i]) + rr[i];
       *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
     } else {  // FDS_CONV_BWD_DATA
-      if (p.resid) {
-        float res[8];
-        unpack8(*reinterpret_cast<const uint4*>(p.resid + o), res);
+      float rr[8], z[8];
+      unpack8(res[g], rr);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] += res[i];
-      }
+      for (int i = 0; i < 8; ++i) v[i] += rr[i];
       if (p.out_h) *reinterpret_cast<uint4*>(p.out_h + o) = pack8(v);
-      float z[8];
       unpack8(*reinterpret_cast<const uint4*>(p.zin + o), z);
 #pragma unroll
       for (int i = 0; i < 8; ++i) v[i] *= gelu_grad(z[i]);
@@ -181,6 +189,8 @@ __device__ void conv_epilogue_row(const ConvDev& p, const Tile& tl, int r, int q
   }
 }
 
+// The epilogue role: warp w handles tensor-memory lane quarter w % 4 (the quarter
+// it may read) of output row (w - 2) / 4 of every tile of the CTA.
 // A bounded wait on an mbarrier phase that every lane of the warp takes together.
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
   const bool ok = mbar_wait(bar, parity, kWaitLimit);
@@ -195,6 +205,91 @@ __device__ __forceinline__ bool aborted(volatile int* flag) {
 // Tiles of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
 __device__ __forceinline__ int my_tiles(int ntiles) {
   return blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+}
+
+// The epilogue role: warp w handles tensor-memory lane quarter w % 4 (the quarter
+// it may read) of output row (w - 2) / 4 of every tile of the CTA.
+template <int NG>
+__device__ void conv_epilogue_role(const ConvDev& p, uint32_t tm, uint64_t* acc_full,
+                                   uint64_t* acc_empty, volatile int* abort_flag,
+                                   const float* bias_s, int nmine) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = warp & 3, r = (warp - 2) >> 2;
+  const size_t plane = (size_t)p.H * p.W;
+  const size_t gstride = plane * 8;
+  for (int k = 0; k < nmine; ++k) {
+    const int a = k & 1, u = k >> 1;
+    if (aborted(abort_flag)) break;
+    const Tile tl = decode_tile(blockIdx.x + k * gridDim.x, p.H, p.W, p.dil, kRows);
+    const size_t pix = (size_t)(tl.y0 + r * p.dil) * p.W + tl.x0 + 32 * q + lane;
+    const size_t o0 = ((size_t)tl.b * NG * plane + pix) * 8;
+    uint4 res[NG];
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+      res[g] = p.resid ? *reinterpret_cast<const uint4*>(p.resid + o0 + g * gstride)
+                       : make_uint4(0u, 0u, 0u, 0u);
+    if (!warp_wait(acc_full + a, (uint32_t)(u & 1))) {
+      if (lane == 0) *abort_flag = 1;
+      break;
+    }
+    tc_fence_after();
+    conv_epilogue_row<NG>(p, o0, gstride,
+                          tm + ((uint32_t)(32 * q) << 16) +
+                              (uint32_t)(a * kRows * kAccStride + r * kAccStride),
+                          bias_s, res);
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(acc_empty + a);
+  }
+}
+
+// The MMA role (one thread issues): per tile and output row r, 9 taps x KC
+// 16-channel chunks accumulate into one tensor-memory accumulator. Descriptors
+// are built once; a tap or chunk only adds its byte offset / 16 to the start
+// address field (addresses stay below 256 KB, so the field cannot carry).
+template <int KC, int NOUT>
+__device__ void conv_mma_role(const ConvDev& p, unsigned char* sm, unsigned char* abuf0,
+                              uint64_t* full, uint64_t* empty, uint64_t* acc_full,
+                              uint64_t* acc_empty, volatile int* abort_flag, uint32_t tm,
+                              int nmine) {
+  const int lane = threadIdx.x & 31;
+  constexpr uint32_t idesc = umma_idesc_bf16(128, NOUT);
+  const uint64_t bdesc0 = umma_desc(smem_addr(sm), NOUT * 16u, 128u);
+  const uint32_t pitch = (uint32_t)p.pitch, dil = (uint32_t)p.dil, slab16 = (uint32_t)p.slab >> 4;
+  int last = -1;
+  for (int k = 0; k < nmine; ++k) {
+    const int s = k & 1, u = k >> 1;
+    if (aborted(abort_flag)) break;
+    if (!warp_wait(full + s, (uint32_t)(u & 1)) ||
+        (u > 0 && !warp_wait(acc_empty + s, (uint32_t)((u - 1) & 1)))) {
+      if (lane == 0) *abort_flag = 1;
+      break;
+    }
+    tc_fence_after();
+    if (lane == 0) {
+      const uint64_t adesc0 = umma_desc(smem_addr(abuf0 + s * p.abuf), (uint32_t)p.slab, 128u);
+      const uint32_t acc0 = tm + (uint32_t)(s * kRows * kAccStride);
+#pragma unroll 1
+      for (int r = 0; r < kRows; ++r) {
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+          const uint32_t arow = (uint32_t)(r + tap / 3) * pitch + (uint32_t)(tap % 3) * dil;
+#pragma unroll
+          for (int kc = 0; kc < KC; ++kc) {
+            umma_bf16(acc0 + r * kAccStride, adesc0 + (arow + 2u * kc * slab16),
+                      bdesc0 + (uint64_t)((tap * KC + kc) * NOUT * 2), idesc,
+                      (tap | kc) != 0 ? 1u : 0u);
+          }
+        }
+      }
+      umma_commit(empty + s);
+      umma_commit(acc_full + s);
+    }
+    __syncwarp();
+    last = k;
+  }
+  if (aborted(abort_flag) && last >= 0)  // MMAs complete in order: wait for the last
+    warp_wait(acc_full + (last & 1), (uint32_t)((last >> 1) & 1));
 }
 
 // Warp roles: warp 0 stages tiles with TMA, warp 1 issues the MMAs, warps 2 ..
@@ -215,10 +310,12 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   uint64_t* acc_empty = bars + 6;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  float* bias_s = reinterpret_cast<float*>(tmem_slot + 4);  // [64]
   if ((smem_addr(sm) & 127u) != 0) {  // TMA destinations need 128-byte alignment
     if (tid == 0 && p.status) atomicOr(p.status, FDS_SURR_STATUS_ALIGN);
     return;
   }
+  if (tid < 64) bias_s[tid] = (p.bias && tid < p.cout) ? p.bias[tid] : 0.0f;
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
       mbar_init(full + i, 1);
@@ -257,7 +354,8 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       if (lane == 0) {
         mbar_arrive_expect_tx(full + s, tx_bytes);
         issue_rows(&xmap, decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kRows), p.dil,
-                   p.cin / 8, kRows + 2, p.rx, p.pitch, p.slab, 1, abuf0 + s * p.abuf, full + s);
+                   p.cin / 8, kRows + 2, p.rx, p.slab, p.pitch * 16, 1, abuf0 + s * p.abuf,
+                   full + s);
       }
       __syncwarp();
       ++issued[s];
@@ -267,60 +365,23 @@ __global__ void __launch_bounds__(kConvThreads, 1)
         if (issued[s] > 0) warp_wait(full + s, (uint32_t)((issued[s] - 1) & 1));
   } else if (warp == 1) {
     // ---- MMA issuer
-    const int KC = p.cin / 16;
-    const uint32_t idesc = umma_idesc_bf16(128, p.cout);
-    const uint32_t w_addr = smem_addr(sm);
-    int last = -1;
-    for (int k = 0; k < nmine; ++k) {
-      const int s = k & 1, u = k >> 1;
-      if (aborted(abort_flag)) break;
-      if (!warp_wait(full + s, (uint32_t)(u & 1)) ||
-          (u > 0 && !warp_wait(acc_empty + s, (uint32_t)((u - 1) & 1)))) {
-        if (lane == 0) *abort_flag = 1;
-        break;
-      }
-      tc_fence_after();
-      if (lane == 0) {
-        const uint32_t a0 = smem_addr(abuf0 + s * p.abuf);
-        const uint32_t acc0 = tm + (uint32_t)(s * kRows * kAccStride);
-        for (int r = 0; r < kRows; ++r) {
-          uint32_t accumulate = 0;
-          for (int tap = 0; tap < 9; ++tap) {
-            const int dy = tap / 3, dx = tap % 3;
-            const uint32_t arow = a0 + (uint32_t)(((r + dy) * p.pitch + dx * p.dil) * 16);
-            for (int kc = 0; kc < KC; ++kc) {
-              const uint32_t a = arow + (uint32_t)(2 * kc * p.slab);
-              const uint32_t b = w_addr + (uint32_t)((tap * KC + kc) * p.cout * 32);
-              umma_bf16(acc0 + r * kAccStride, umma_desc(a, (uint32_t)p.slab, 128u),
-                        umma_desc(b, (uint32_t)(p.cout * 16), 128u), idesc, accumulate);
-              accumulate = 1;
-            }
-          }
-        }
-        umma_commit(empty + s);
-        umma_commit(acc_full + s);
-      }
-      __syncwarp();
-      last = k;
+    switch (p.cin * 4 + p.cout / 16) {
+      case 16 * 4 + 1: conv_mma_role<1, 16>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 16 * 4 + 2: conv_mma_role<1, 32>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 16 * 4 + 3: conv_mma_role<1, 48>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 32 * 4 + 1: conv_mma_role<2, 16>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 32 * 4 + 2: conv_mma_role<2, 32>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 32 * 4 + 3: conv_mma_role<2, 48>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 48 * 4 + 1: conv_mma_role<3, 16>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      case 48 * 4 + 2: conv_mma_role<3, 32>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
+      default: conv_mma_role<3, 48>(p, sm, abuf0, full, empty, acc_full, acc_empty, abort_flag, tm, nmine); break;
     }
-    if (aborted(abort_flag) && last >= 0)  // MMAs complete in order: wait for the last
-      warp_wait(acc_full + (last & 1), (uint32_t)((last >> 1) & 1));
   } else {
     // ---- epilogue
-    const int q = warp & 3, r = (warp - 2) >> 2;
-    for (int k = 0; k < nmine; ++k) {
-      const int a = k & 1, u = k >> 1;
-      if (aborted(abort_flag)) break;
-      if (!warp_wait(acc_full + a, (uint32_t)(u & 1))) {
-        if (lane == 0) *abort_flag = 1;
-        break;
-      }
-      tc_fence_after();
-      conv_epilogue_row(p, decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kRows), r, q,
-                        tm + (uint32_t)(a * kRows * kAccStride));
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty + a);
+    switch (p.cout) {
+      case 16: conv_epilogue_role<2>(p, tm, acc_full, acc_empty, abort_flag, bias_s, nmine); break;
+      case 32: conv_epilogue_role<4>(p, tm, acc_full, acc_empty, abort_flag, bias_s, nmine); break;
+      default: conv_epilogue_role<6>(p, tm, acc_full, acc_empty, abort_flag, bias_s, nmine); break;
     }
   }
   tc_fence_before();
@@ -332,12 +393,56 @@ __global__ void __launch_bounds__(kConvThreads, 1)
 
 // ------------------------------------------------------------------ weight gradient
 
+// Shared memory of a weight-gradient stage: the input rows as [row][group][pixel][8]
+// (group stride pitch * 16 bytes, row stride xrow = cin/8 groups), so that the
+// 8-channel groups of three consecutive rows (taps dy = 0, 1, 2) are N-groups at a
+// constant stride of one MMA; then the gradient rows as [group][row][128][8].
 struct WgradDev {
   float* partial;
   int32_t* status;
   int B, H, W, cin, cout, dil, ntiles;
-  int rx, pitch, xslab, dzslab, xbytes, buf;
+  int rx, pitch, xrow, dzslab, xbytes, buf;
 };
+
+// The weight-gradient MMA role (one thread issues): per tile, output row r and
+// 16-pixel window, one MMA per horizontal tap dx (M = 64 output channels, N = 3 cin
+// = the three vertical taps x cin, K = 16 pixels, both operands MN-major) into the
+// accumulator of that dx; descriptors are built once and advanced by offset / 16.
+template <int CIN>
+__device__ void wgrad_mma_role(const WgradDev& p, unsigned char* sm, uint64_t* full, uint64_t* empty,
+                               volatile int* abort_flag, uint32_t tm, int nmine) {
+  const int lane = threadIdx.x & 31;
+  constexpr uint32_t idesc = umma_idesc_bf16(64, 3 * CIN) | kUmmaAMajorMN | kUmmaBMajorMN;
+  const uint32_t pitch = (uint32_t)p.pitch, dil = (uint32_t)p.dil;
+  const uint32_t row16 = (uint32_t)p.xrow >> 4;
+  for (int k = 0; k < nmine; ++k) {
+    const int s = k & 1, u = k >> 1;
+    if (aborted(abort_flag) || !warp_wait(full + s, (uint32_t)(u & 1))) {
+      if (lane == 0) *abort_flag = 1;
+      break;
+    }
+    tc_fence_after();
+    if (lane == 0) {
+      const uint32_t xb = smem_addr(sm + s * p.buf);
+      const uint64_t zd0 = umma_desc(xb + (uint32_t)p.xbytes, 128u, (uint32_t)p.dzslab);
+      const uint64_t xd0 = umma_desc(xb, 128u, pitch * 16u);
+#pragma unroll 1
+      for (int r = 0; r < kWRows; ++r)
+#pragma unroll 1
+        for (int w16 = 0; w16 < kTilePx / 16; ++w16) {
+          const uint64_t ad = zd0 + (uint64_t)(r * kTilePx + w16 * 16);
+          const uint32_t acc = (k > 0 || r > 0 || w16 > 0) ? 1u : 0u;
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx) {
+            const uint32_t off = (uint32_t)r * row16 + (uint32_t)(w16 * 16) + (uint32_t)dx * dil;
+            umma_bf16(tm + (uint32_t)(dx * 3 * CIN), ad, xd0 + off, idesc, acc);
+          }
+        }
+      umma_commit(empty + s);
+    }
+    __syncwarp();
+  }
+}
 
 // Warp roles: warp 0 stages tiles (input rows and gradient rows) with TMA, warp 1
 // issues the MMAs (every tile of the CTA accumulates into the same 9 per-tap
@@ -395,8 +500,9 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
         const Tile tl = decode_tile(blockIdx.x + k * grid, p.H, p.W, p.dil, kWRows);
         unsigned char* base = sm + s * p.buf;
         mbar_arrive_expect_tx(full + s, tx_bytes);
-        issue_rows(&xmap, tl, p.dil, KGx, kWRows + 2, p.rx, p.pitch, p.xslab, 1, base, full + s);
-        issue_rows(&dzmap, tl, p.dil, KGz, kWRows, kTilePx, kTilePx, p.dzslab, 0,
+        issue_rows(&xmap, tl, p.dil, KGx, kWRows + 2, p.rx, p.pitch * 16, p.xrow, 1, base,
+                   full + s);
+        issue_rows(&dzmap, tl, p.dil, KGz, kWRows, kTilePx, p.dzslab, kTilePx * 16, 0,
                    base + p.xbytes, full + s);
       }
       __syncwarp();
@@ -406,32 +512,10 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
       for (int s = 0; s < 2; ++s)
         if (issued[s] > 0) warp_wait(full + s, (uint32_t)((issued[s] - 1) & 1));
   } else if (warp == 1) {
-    const uint32_t idesc = umma_idesc_bf16(64, p.cin) | kUmmaAMajorMN | kUmmaBMajorMN;
-    for (int k = 0; k < nmine; ++k) {
-      const int s = k & 1, u = k >> 1;
-      if (aborted(abort_flag) || !warp_wait(full + s, (uint32_t)(u & 1))) {
-        if (lane == 0) *abort_flag = 1;
-        break;
-      }
-      tc_fence_after();
-      if (lane == 0) {
-        const uint32_t xb = smem_addr(sm + s * p.buf);
-        const uint32_t zb = xb + (uint32_t)p.xbytes;
-        for (int r = 0; r < kWRows; ++r)
-          for (int w16 = 0; w16 < kTilePx / 16; ++w16) {
-            const uint32_t a = zb + (uint32_t)((r * kTilePx + w16 * 16) * 16);
-            const uint64_t ad = umma_desc(a, 128u, (uint32_t)p.dzslab);
-            for (int tap = 0; tap < 9; ++tap) {
-              const int dy = tap / 3, dx = tap % 3;
-              const uint32_t b =
-                  xb + (uint32_t)(((r + dy) * p.pitch + w16 * 16 + dx * p.dil) * 16);
-              umma_bf16(tm + (uint32_t)(tap * p.cin), ad, umma_desc(b, 128u, (uint32_t)p.xslab),
-                        idesc, (k > 0 || r > 0 || w16 > 0) ? 1u : 0u);
-            }
-          }
-        umma_commit(empty + s);
-      }
-      __syncwarp();
+    switch (p.cin) {
+      case 16: wgrad_mma_role<16>(p, sm, full, empty, abort_flag, tm, nmine); break;
+      case 32: wgrad_mma_role<32>(p, sm, full, empty, abort_flag, tm, nmine); break;
+      default: wgrad_mma_role<48>(p, sm, full, empty, abort_flag, tm, nmine); break;
     }
     // completion of every MMA of this CTA (also when there were none, or on abort)
     if (lane == 0) umma_commit(done);
@@ -463,7 +547,8 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   const bool ok = !*abort_flag && warp_wait(done, 0u);
   tc_fence_after();
   if (ok && warp >= 2) {
-    // D row m (output channel) sits in lane 32 (m / 16) + m % 16
+    // D row m (output channel) sits in lane 32 (m / 16) + m % 16; tap (dy, dx) is
+    // columns (3 dx + dy) cin .. + cin - 1
     const int q = warp & 3, half = (warp - 2) >> 2;
     const int m = 16 * q + lane;
     const int hc = p.cin / 2;
@@ -473,7 +558,9 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
       for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 8) {
         float v[8];
         if (nmine > 0) {
-          tmem_ld8(tm + ((uint32_t)(32 * q) << 16) + (uint32_t)(tap * p.cin + c0), v);
+          tmem_ld8(tm + ((uint32_t)(32 * q) << 16) +
+                       (uint32_t)((3 * (tap % 3) + tap / 3) * p.cin + c0),
+                   v);
         } else {
 #pragma unroll
           for (int i = 0; i < 8; ++i) v[i] = 0.0f;
@@ -803,7 +890,7 @@ extern "C" int32_t fds_conv3x3(const FdsConvArgs* a, void* stream) {
   p.slab = (kRows + 2) * p.pitch * 16;
   p.abuf = (a->cin / 8) * p.slab;
   p.wbytes = 9 * a->cin * a->cout * 2;
-  const int smem = round_up(p.wbytes, 128) + 2 * p.abuf + 64;
+  const int smem = round_up(p.wbytes, 128) + 2 * p.abuf + 96 + 64 * 4;
   if (smem > kMaxSmem)
     return set_error(FDS_E_SIZE, "convolution %d->%d dilation %d needs %d bytes of shared memory",
                      a->cin, a->cout, a->dilation, smem);
@@ -847,9 +934,9 @@ extern "C" int32_t fds_conv3x3_wgrad(const FdsWgradArgs* a, void* stream) {
   p.ntiles = a->batch * (a->height / (kWRows * a->dilation)) * a->dilation * (a->width / kTilePx);
   p.rx = kTilePx + 2 * a->dilation;
   p.pitch = round_up(p.rx, 8);
-  p.xslab = (kWRows + 2) * p.pitch * 16;
+  p.xrow = (a->cin / 8) * p.pitch * 16;
   p.dzslab = kWRows * kTilePx * 16;
-  p.xbytes = (a->cin / 8) * p.xslab;
+  p.xbytes = (kWRows + 2) * p.xrow;
   // the M = 64 operand spans 8 channel groups; the ones past cout are never used
   p.buf = p.xbytes + 8 * p.dzslab;
   const int smem = 2 * p.buf + 64 + kBiasWarps * 64 * 4;
