@@ -650,31 +650,53 @@ __device__ __forceinline__ const T* state_at(const FdsSurrData& d, int k, int sn
          ((size_t)d.inst[k] * d.nsnap + d.snap[k] + snap_shift) * 3 * plane;
 }
 
-// Block-wide sum (blockDim.x == 256), the same order on every call.
+// Block-wide sum over blockDim.x = 32 * NW threads, the same order on every call.
+template <int NW>
 __device__ __forceinline__ float block_sum(float v, float* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   float s = 0.0f;
   if (threadIdx.x == 0)
-    for (int w = 0; w < 8; ++w) s += red[w];
+    for (int w = 0; w < NW; ++w) s += red[w];
   __syncthreads();
   return s;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) scale_kernel(const FdsSurrData d) {
-  __shared__ float red[8];
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using type = float4;
+};
+template <>
+struct Vec4<double> {
+  using type = double4;
+};
+
+// Energy norm of each sample's input state: one 1024-thread CTA per sample, four
+// cells per load (the plane is a multiple of 128 cells).
+template <typename T>
+__global__ void __launch_bounds__(1024) scale_kernel(const FdsSurrData d) {
+  __shared__ float red[32];
+  using V = typename Vec4<T>::type;
   const int k = blockIdx.x;
   const size_t plane = (size_t)d.height * d.width;
   const T* st = state_at<T>(d, k, 0);
   const float z = d.zref[d.inst[k]];
+  const V* p4 = reinterpret_cast<const V*>(st);
+  const V* x4 = reinterpret_cast<const V*>(st + plane);
+  const V* y4 = reinterpret_cast<const V*>(st + 2 * plane);
   float acc = 0.0f;
-  for (size_t i = threadIdx.x; i < plane; i += blockDim.x) {
-    const float pv = (float)st[i], vx = z * (float)st[plane + i], vy = z * (float)st[2 * plane + i];
-    acc += pv * pv + vx * vx + vy * vy;
+  for (size_t i = threadIdx.x; i < plane / 4; i += blockDim.x) {
+    const V a = p4[i], b = x4[i], c = y4[i];
+    acc += (float)a.x * (float)a.x + (float)a.y * (float)a.y + (float)a.z * (float)a.z +
+           (float)a.w * (float)a.w;
+    const float bx = z * (float)b.x, by = z * (float)b.y, bz = z * (float)b.z, bw = z * (float)b.w;
+    const float cx = z * (float)c.x, cy = z * (float)c.y, cz = z * (float)c.z, cw = z * (float)c.w;
+    acc += bx * bx + by * by + bz * bz + bw * bw + cx * cx + cy * cy + cz * cz + cw * cw;
   }
-  const float s = block_sum(acc, red);
+  const float s = block_sum<32>(acc, red);
   if (threadIdx.x == 0) d.scale[k] = sqrtf(s / (float)plane);
 }
 
@@ -726,7 +748,7 @@ __global__ void __launch_bounds__(256)
     g[k * 2 * plane + pix] = pack8(f);
     g[(k * 2 + 1) * plane + pix] = make_uint4(0u, 0u, 0u, 0u);
   }
-  const float s = block_sum(err, red);
+  const float s = block_sum<8>(err, red);
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
 }
 
@@ -1012,10 +1034,10 @@ extern "C" int32_t fds_surr_pack(const FdsSurrData* d, void* stream) {
   const size_t plane = (size_t)d->height * d->width;
   const dim3 grid((unsigned)((plane + 255) / 256), (unsigned)d->count);
   if (d->state_f64) {
-    scale_kernel<double><<<d->count, 256, 0, s>>>(*d);
+    scale_kernel<double><<<d->count, 1024, 0, s>>>(*d);
     pack_input_kernel<double><<<grid, 256, 0, s>>>(*d);
   } else {
-    scale_kernel<float><<<d->count, 256, 0, s>>>(*d);
+    scale_kernel<float><<<d->count, 1024, 0, s>>>(*d);
     pack_input_kernel<float><<<grid, 256, 0, s>>>(*d);
   }
   return launch_error("pack_input_kernel");
