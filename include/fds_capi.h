@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FDS_ABI_VERSION 1
+#define FDS_ABI_VERSION 2
 
 /* error codes */
 #define FDS_OK 0
@@ -57,6 +57,10 @@ extern "C" {
 #define FDS_FLAG_AXI 4u     /* axisymmetric: x is the radius (Acoustic3DAxi / Thermal3DAxi) */
 #define FDS_FLAG_EXACT 8u   /* F64 only: reproduce the reference's floating-point
                               operation order exactly (no fused multiply-add) */
+#define FDS_FLAG_FLOW 16u   /* acoustic 2-D with a moving medium (AcousticFlow2D): after
+                              each step, rows y with flow_period[y] == 0 or
+                              step % flow_period[y] == 0 move one cell in +x (their
+                              first cell becomes 0) in p, vx and vy */
 
 /* Boundary operation flags (FdsBoundOp.flags) */
 #define FDS_BOP_SIGNAL 2 /* value = pool[off + step * stride]  (else value = scalar) */
@@ -112,6 +116,8 @@ typedef struct FdsStagProblem {
                      (finer float spacing near a reference temperature); the flux
                      adds the reference's interface term -(b_i - b_i-1) * offset, and
                      boundary values / outputs are shifted by the caller. 0 otherwise */
+  const int64_t* flow_period; /* FDS_FLAG_FLOW: [ny] device array of shift periods in
+                                 steps, int(dx / flow / dt) per row; NULL otherwise */
 } FdsStagProblem;
 
 /*
@@ -218,6 +224,12 @@ int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, in
 int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps,
                      int32_t store_flux, void* stream);
+
+/* The moving-medium shift of one step alone, in place on state->cur (p, vx, vy):
+ * replaces AcousticFlow2D.apply_flow (pyfds/acoustic_flow.py:49-57) for callers that
+ * step a flow field themselves. Needs FDS_FLAG_FLOW and flow_period. */
+int32_t fds_stag_flow_shift(const FdsStagProblem* prob, FdsStagState* state, int64_t step,
+                            void* stream);
 
 /* Workspace (device bytes, 256-byte aligned) a batched call over `count` instances
  * with `total_tiles` tiles in all needs: per-instance descriptors and the work

@@ -34,9 +34,14 @@ def run(nsteps):
     bounds = spec.get("bounds") or {}
     signals = {c: [[[] for _ in idx] for idx in outputs.get(c, [])]
                for c in O.components_of(spec["kind"])}
+    kind = spec["kind"]
+    periods = O.flow_periods(spec) if kind == "AcousticFlow2D" else None
+    step_kind = "Acoustic2D" if periods is not None else kind
     t0 = time.perf_counter()
     for _ in range(nsteps):
-        O.sim_step(spec["kind"], ops, state, bounds, outputs, signals, _W["step"], dt=spec["dt"])
+        O.sim_step(step_kind, ops, state, bounds, outputs, signals, _W["step"], dt=spec["dt"])
+        if periods is not None:
+            O.apply_flow(state, periods, _W["step"], ops["nx"])
         _W["step"] += 1
     return time.perf_counter() - t0
 

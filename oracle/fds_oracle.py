@@ -186,6 +186,7 @@ def components_of(kind):
     return {
         "Acoustic1D": ["pressure", "velocity"],
         "Acoustic2D": ["pressure", "velocity_x", "velocity_y"],
+        "AcousticFlow2D": ["pressure", "velocity_x", "velocity_y"],
         "Acoustic3DAxi": ["pressure", "velocity_x", "velocity_y"],
         "Thermal1D": ["temperature", "heat_flux"],
         "Thermal2D": ["temperature", "heat_flux_x", "heat_flux_y"],
@@ -216,6 +217,8 @@ def assemble(spec):
         return material_vector(n, mats, name)
 
     ops = {"n": n, "nx": nx}
+    if kind == "AcousticFlow2D":
+        kind = "Acoustic2D"  # pyfds/acoustic_flow.py:13: the Acoustic2D operators
     if kind == "Acoustic1D":
         # pyfds/acoustics.py:27-38
         ops["a_p_v"] = d_x(n, dt / dx * mv("sound_velocity") ** 2 * mv("density"))
@@ -382,6 +385,33 @@ def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
         raise ValueError("unknown field kind %r" % kind)
 
 
+def flow_periods(spec):
+    """``AcousticFlow2D.flow_t_deltas`` (pyfds/acoustic_flow.py:27-37): per row, the
+    step period of the one-cell shift, ``int(dx / flow / dt)``."""
+    flow, ny = spec["flow"], spec["ny"]
+    if isinstance(flow, (list, np.ndarray)) and len(flow) == ny:
+        f = np.asarray(flow)
+    elif isinstance(flow, (float, int)):
+        f = np.ones(ny) * flow
+    else:
+        raise ValueError('Flow must either be scalar or a vector with length of y_samples.')
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return (spec["dx"] / f / spec["dt"]).astype(int)
+
+
+def apply_flow(state, periods, step, nx):
+    """``AcousticFlow2D.apply_flow`` (pyfds/acoustic_flow.py:49-57): rows whose period
+    divides the step move one cell in +x, their first cell becomes 0."""
+    for c in ("pressure", "velocity_x", "velocity_y"):
+        v = state[c]
+        for n, f in enumerate(periods):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                due = step % f == 0
+            if due:
+                v[n * nx + 1:(n + 1) * nx] = v[n * nx:(n + 1) * nx - 1]
+                v[n * nx:n * nx + 1] = 0
+
+
 def simulate(spec, num_steps=None, state=None, step0=0):
     """Run ``num_steps`` steps of the scenario ``spec`` (``Field.simulate``,
     pyfds/fields.py:67-95: assemble once, then ``sim_step(); step += 1``).
@@ -402,8 +432,12 @@ def simulate(spec, num_steps=None, state=None, step0=0):
     bounds = spec.get("bounds") or {}
     outputs = spec.get("outputs") or {}
     signals = {c: [[[] for _ in idx] for idx in outputs.get(c, [])] for c in components_of(kind)}
+    periods = flow_periods(spec) if kind == "AcousticFlow2D" else None
+    step_kind = "Acoustic2D" if kind == "AcousticFlow2D" else kind
     for s in range(step0, step0 + num_steps):
-        sim_step(kind, ops, state, bounds, outputs, signals, s, dt=spec["dt"])
+        sim_step(step_kind, ops, state, bounds, outputs, signals, s, dt=spec["dt"])
+        if periods is not None:
+            apply_flow(state, periods, s, ops["nx"])
     out = {c: [np.array(sig, dtype=np.float64).reshape(len(sig), -1) for sig in signals[c]]
            for c in signals}
     return state, out

@@ -41,7 +41,8 @@ def build_reference_field(spec):
         fld = cls(x_samples=spec["nx"], x_delta=spec["dx"], t_samples=spec["nt"],
                   t_delta=spec["dt"], material=main)
     else:
-        fld = cls(x_samples=spec["nx"], x_delta=spec["dx"], y_samples=spec["ny"],
+        extra = (spec["flow"],) if kind == "AcousticFlow2D" else ()
+        fld = cls(*extra, x_samples=spec["nx"], x_delta=spec["dx"], y_samples=spec["ny"],
                   y_delta=spec["dy"], t_samples=spec["nt"], t_delta=spec["dt"], material=main)
     for indices, params in mats[1:]:
         fld.add_material_region(reg.Region(list(map(int, indices)), "mat"),

@@ -125,3 +125,22 @@ def random_scenario(seed, kind, nx, ny=None, steps=40, mu=True, boundary_modes="
         spec["ny"] = ny
         spec["dy"] = dy
     return spec
+
+
+def flow_scenario(seed, nx, ny, steps=60, flow="rows", mu=True):
+    """A random Acoustic2D scenario with a moving medium (``AcousticFlow2D``,
+    pyfds/acoustic_flow.py:13-57): the random_scenario of Acoustic2D plus a flow
+    velocity, per row (``flow="rows"``: periods 1..9 steps, some rows negative and
+    one row at rest) or one scalar (``flow="scalar"``)."""
+    spec = random_scenario(seed, "Acoustic2D", nx, ny, steps=steps, mu=mu)
+    rng = np.random.default_rng(seed + 7919)
+    spec["kind"] = "AcousticFlow2D"
+    if flow == "scalar":
+        spec["flow"] = float(spec["dx"] / spec["dt"] / rng.integers(2, 7))
+    else:
+        periods = rng.integers(1, 10, size=ny).astype(np.float64)
+        periods[rng.random(ny) < 0.2] *= -1
+        v = spec["dx"] / spec["dt"] / (periods + 0.25)
+        v[rng.integers(0, ny)] = 0.0
+        spec["flow"] = v
+    return spec

@@ -12,7 +12,7 @@ import numpy as np
 
 from ._build import LIB_PATH
 
-FDS_ABI_VERSION = 1
+FDS_ABI_VERSION = 2
 
 FDS_OK = 0
 FDS_E_ARG = -1
@@ -32,13 +32,14 @@ FLAG_HAS_V = 1
 FLAG_ABSORB = 2
 FLAG_AXI = 4
 FLAG_EXACT = 8
+FLAG_FLOW = 16
 
 BOP_SIGNAL = 2
 
 # exported symbols, in header order
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
-                    "fds_stag_batch_run", "fds_stag_batch_run_static",
+                    "fds_stag_batch_run", "fds_stag_batch_run_static", "fds_stag_flow_shift",
                     # include/fds_surrogate.h
                     "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
                     "fds_conv_wgrad_max_grid", "fds_adamw", "fds_surr_pack", "fds_surr_loss",
@@ -60,7 +61,7 @@ class FdsStagProblem(C.Structure):
     _fields_ = [("family", C.c_int32), ("precision", C.c_int32), ("flags", C.c_uint32),
                 ("nx", C.c_int32), ("ny", C.c_int32), ("tile_x", C.c_int32),
                 ("tile_y", C.c_int32), ("stages", C.c_int32), ("coefs", FdsCoefs),
-                ("offset", C.c_double)]
+                ("offset", C.c_double), ("flow_period", C.c_void_p)]
 
 
 class FdsStagState(C.Structure):
@@ -180,6 +181,12 @@ def load(path=None):
     lib.fds_stag_batch_run_static.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                               C.POINTER(FdsStagTables), C.c_int32, C.c_int64,
                                               C.c_int32, C.c_int32, C.c_void_p]
+    lib.fds_stag_flow_shift.restype = C.c_int32
+    lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
+                                        C.c_int64, C.c_void_p]
+    lib.fds_stag_flow_shift.restype = C.c_int32
+    lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
+                                        C.c_int64, C.c_void_p]
     # include/fds_surrogate.h
     P = C.c_void_p
     lib.fds_conv3x3.restype = C.c_int32

@@ -95,6 +95,30 @@ class StagEngine:
                 np.ascontiguousarray(arr, dtype=np.float64)).to(dev).to(tc)
         self.coef_key = key
 
+    def _flow_periods(self, torch, dev):
+        """Device copy (int64) of a moving-medium field's per-row shift periods."""
+        per = np.ascontiguousarray(self.field._flow_periods(), dtype=np.int64)
+        cached = getattr(self, "_flow_cache", None)
+        if cached is None or not np.array_equal(cached[0], per):
+            self._flow_cache = (per.copy(), torch.from_numpy(per).to(dev))
+        return self._flow_cache[1]
+
+    def flow_shift(self, step):
+        """The moving-medium shift of ``step`` on the device state (fds_stag_flow_shift)."""
+        torch = require_cuda()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        plan = self.prepare(step, 0)
+        state = _capi.FdsStagState()
+        for k, name in enumerate(self.field._stag_components):
+            cur, nxt = self.buffers[name]
+            state.cur[k] = cur.data_ptr()
+            state.nxt[k] = nxt.data_ptr()
+        lib = _capi.load()
+        _capi.check(lib.fds_stag_flow_shift(C.byref(plan["prob"]), C.byref(state), int(step),
+                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        for name in self.field._stag_components:
+            getattr(self.field, name)._where = "device"
+
     # ------------------------------------------------------------------- state
     def _potential_offset(self):
         """Offset of the stored potential: float32 thermal fields keep T - T_ref, with
@@ -257,6 +281,8 @@ class StagEngine:
         for name in ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx"):
             t = self.coef_tensors.get(name)
             setattr(prob.coefs, name, t.data_ptr() if t is not None else None)
+        if prob.flags & _capi.FLAG_FLOW:
+            prob.flow_period = self._flow_periods(torch, dev).data_ptr()
         if self.status is None:
             self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         tstruct = self._tables_struct(tabs, outs, nsteps)

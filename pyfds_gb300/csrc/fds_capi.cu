@@ -100,6 +100,11 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
   if ((prob->flags & FDS_FLAG_AXI) && !c.rx) return set_error(FDS_E_ARG, "axisymmetric field without radii");
   if ((prob->flags & FDS_FLAG_AXI) && (prob->flags & FDS_FLAG_ABSORB) && !c.ex)
     return set_error(FDS_E_ARG, "axisymmetric absorption without its radial loss factor");
+  if ((prob->flags & FDS_FLAG_FLOW) &&
+      (prob->family != FDS_FAMILY_ACOUSTIC || !has_v || (prob->flags & FDS_FLAG_AXI) ||
+       !prob->flow_period || prob->precision == FDS_PREC_F32_T64))
+    return set_error(FDS_E_ARG, "flow needs a 2-D Cartesian float64/float32 acoustic field "
+                                "and its flow_period array");
   const int ncomp = has_v ? 3 : 2;
   for (int k = 0; k < ncomp; ++k)
     if (!state->cur[k] || !state->nxt[k]) return set_error(FDS_E_ARG, "missing state buffer %d", k);
@@ -153,7 +158,7 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
         p.tile_x != p0.tile_x || p.tile_y != p0.tile_y || p.stages != p0.stages)
       return set_error(FDS_E_ARG, "instance %d differs from instance 0 in variant or tile", i);
     if (p.nx < 1 || p.ny < 1) return set_error(FDS_E_ARG, "instance %d: bad grid", i);
-    if (!(p.flags & FDS_FLAG_HAS_V) || (p.flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT)))
+    if (!(p.flags & FDS_FLAG_HAS_V) || (p.flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT | FDS_FLAG_FLOW)))
       return set_error(FDS_E_NOKERNEL, "batched runs cover lossless 2-D non-exact fields");
     if (!p.coefs.bx || !p.coefs.kx) return set_error(FDS_E_ARG, "instance %d: missing coefficients", i);
     for (int k = 0; k < 3; ++k)

@@ -35,4 +35,8 @@ int32_t run_batch_f32t64(const FdsStagProblem*, FdsStagState*, const FdsStagTabl
                          void*, size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);
 size_t batch_workspace_bytes(int32_t count, int64_t total_tiles);
 
+// The moving-medium row shift of one step on the current state (flow.cu).
+int32_t launch_flow_shift(const FdsStagProblem* prob, void* const* cur, int64_t step,
+                          cudaStream_t stream);
+
 }  // namespace fds

@@ -685,7 +685,7 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
 template <typename TP>
 __global__ void __launch_bounds__(1024) stag_prologue_kernel(TP* p, FdsCompTables tb,
                                                              const double* pool, int64_t step,
-                                                             int32_t ntiles) {
+                                                             int32_t ntiles, int64_t row) {
   if (tb.bound_tile_start != nullptr) {
     const int e = tb.bound_tile_start[ntiles];
     for (int g = threadIdx.x; g < e; g += blockDim.x) {
@@ -706,7 +706,7 @@ __global__ void __launch_bounds__(1024) stag_prologue_kernel(TP* p, FdsCompTable
     const int e = tb.probe_tile_start[ntiles];
     for (int q = threadIdx.x; q < e; q += blockDim.x) {
       const FdsProbe pr = tb.probes[q];
-      tb.out[pr.col] = (double)p[pr.cell];
+      tb.out[row * (int64_t)tb.ncols + pr.col] = (double)p[pr.cell];
     }
   }
 }

@@ -197,6 +197,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   const bool absorb = (prob->flags & FDS_FLAG_ABSORB) != 0;
   const bool axi = (prob->flags & FDS_FLAG_AXI) != 0;
   const bool exact = (prob->flags & FDS_FLAG_EXACT) != 0;
+  const bool flow = (prob->flags & FDS_FLAG_FLOW) != 0;
   // stages: 0 (automatic) and 1 = one CTA per tile; 2 = the persistent two-stage
   // pipeline (built for the tile menu; measured slower on GB300 for one field)
   StagLaunch<TP, TF, TC> fn = nullptr;
@@ -253,7 +254,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   const FdsCompTables& t0 = tabs->comp[0];
   if (nsteps > 0 && (t0.bound_tile_start || t0.probe_tile_start)) {
     stag_prologue_kernel<TP><<<1, 1024, 0, stream>>>((TP*)st->cur[0], t0, tabs->pool, step0,
-                                                      ntiles);
+                                                      ntiles, 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
   }
@@ -265,13 +266,26 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
     a.v_in = (const TF*)st->cur[2];
     a.v_out = (TF*)st->nxt[2];
     a.step = step0 + s;
-    a.apply_next = (s + 1 < nsteps) ? 1 : 0;
+    // a moving medium shifts rows between the pressure update and the next step's
+    // pressure bounds / probes, which then run in the prologue kernel instead
+    a.apply_next = (s + 1 < nsteps && !flow) ? 1 : 0;
     a.store_flux = (store_flux || s + 1 == nsteps) ? 1 : 0;
     const int32_t rc = fn(a, stream, &tma);
     if (rc != FDS_OK) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "step launch: %s", cudaGetErrorString(e));
     for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+    if (flow) {
+      const int32_t rf = launch_flow_shift(prob, st->cur, step0 + s, stream);
+      if (rf != FDS_OK) return rf;
+      if (s + 1 < nsteps && (t0.bound_tile_start || t0.probe_tile_start)) {
+        stag_prologue_kernel<TP><<<1, 1024, 0, stream>>>((TP*)st->cur[0], t0, tabs->pool,
+                                                          step0 + s + 1, ntiles, s + 1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+          return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
+      }
+    }
   }
   return FDS_OK;
 }

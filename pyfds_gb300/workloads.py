@@ -13,7 +13,7 @@ field; the same spec drives the CPU oracle in the tests.
 """
 import numpy as np
 
-from . import acoustics, regions as reg, thermal
+from . import acoustic_flow, acoustics, regions as reg, thermal
 
 WATER = {"sound_velocity": 1500.0, "density": 1000.0, "absorption_coef": 0}
 STEEL = {"sound_velocity": 5900.0, "density": 7850.0, "absorption_coef": 0}
@@ -73,6 +73,16 @@ def acoustic2d_steel_block(n=2048, nt=4000, n_probes=64, seed=2):
                 {"indices": edges, "value": 0, "additive": False},
                 {"indices": line, "value": gauss_pulse(t, 1e6, 2e-6, 0.5e-6), "additive": True}]},
             "outputs": {"pressure": [probes]}}
+
+
+def acoustic_flow_block(n=2048, nt=4000, n_probes=64, seed=2, period=10):
+    """The water/steel Acoustic2D workload of ``acoustic2d_steel_block`` in a medium
+    moving along x (AcousticFlow2D): flow = dx / (period + 0.5) / dt in every row, so
+    every row moves one cell every ``period`` steps."""
+    spec = acoustic2d_steel_block(n, nt, n_probes, seed)
+    spec["kind"] = "AcousticFlow2D"
+    spec["flow"] = float(spec["dx"] / (period + 0.5) / spec["dt"])
+    return spec
 
 
 def axi_disc_source(nr=1024, nz=4096, nt=6000, disc=200, probe_every=64):
@@ -237,14 +247,16 @@ def build_field(spec, **kwargs):
     """A pyfds_gb300 field built from a scenario spec (extra kwargs go to the
     constructor, e.g. ``precision`` or ``exact``)."""
     kind = spec["kind"]
-    cls = getattr(acoustics, kind, None) or getattr(thermal, kind)
+    cls = (getattr(acoustics, kind, None) or getattr(acoustic_flow, kind, None)
+           or getattr(thermal, kind))
     mats = spec["materials"]
     main = _material(kind, mats[0][1])
     if kind.endswith("1D"):
         f = cls(x_samples=spec["nx"], x_delta=spec["dx"], t_samples=spec["nt"],
                 t_delta=spec["dt"], material=main, **kwargs)
     else:
-        f = cls(x_samples=spec["nx"], x_delta=spec["dx"], y_samples=spec["ny"],
+        extra = (spec["flow"],) if kind == "AcousticFlow2D" else ()
+        f = cls(*extra, x_samples=spec["nx"], x_delta=spec["dx"], y_samples=spec["ny"],
                 y_delta=spec["dy"], t_samples=spec["nt"], t_delta=spec["dt"], material=main,
                 **kwargs)
     for idx, params in mats[1:]:

@@ -20,6 +20,8 @@ source is not modified. Fixtures:
   workloads (500 steps), outputs and final-state norms.
 - axi_disc_full_prefix.npz, thermal2d_4096_prefix.npz: the full-size axisymmetric
   and thermal workloads for their first 100 steps (--skip-large skips them).
+- acoustic_flow.npz: AcousticFlow2D (moving medium) scenarios, oracle/scenarios.py
+  ``flow_scenario``: per-row and scalar flows, periods 1..9, negative and zero flows.
 """
 import argparse
 import json
@@ -49,6 +51,13 @@ for _seed in range(36):
         _nx, _ny = [5, 7, 3, 11, 2, 9][_seed % 6], [4, 6, 9, 3, 5, 8][(_seed // 6) % 6]
     RANDOM_CASES.append({"seed": _seed, "kind": _kind, "nx": _nx, "ny": _ny, "steps": 30,
                          "mu": _seed % 3 != 0})
+
+
+FLOW_CASES = [{"seed": 200 + k, "nx": nx, "ny": ny, "steps": 45, "flow": fl, "mu": mu}
+              for k, (nx, ny, fl, mu) in enumerate([(9, 7, "rows", True), (16, 5, "rows", False),
+                                                    (7, 11, "scalar", True), (33, 4, "rows", True),
+                                                    (5, 9, "scalar", False), (12, 12, "rows", False),
+                                                    (64, 3, "rows", True)])]
 
 
 def run_and_pack(spec, prefix, out, keep_state=True, steps=None, materials=False):
@@ -103,6 +112,21 @@ def make_random():
     np.savez_compressed(os.path.join(HERE, "random_scenarios.npz"), **out)
 
 
+def make_flow():
+    import warnings
+    out = {}
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")  # the reference warns about high flow velocities
+        for case in FLOW_CASES:
+            spec = scenarios.flow_scenario(case["seed"], case["nx"], case["ny"],
+                                           steps=case["steps"], flow=case["flow"], mu=case["mu"])
+            prefix = "f%d/" % case["seed"]
+            out[prefix + "digest"] = np.array(spec_digest(spec))
+            run_and_pack(spec, prefix, out, materials=True)
+    out["cases"] = np.array(json.dumps(FLOW_CASES))
+    np.savez_compressed(os.path.join(HERE, "acoustic_flow.npz"), **out)
+
+
 def make_workload(name, spec, keep_state, steps=None):
     t0 = time.time()
     out = {"digest": np.array(spec_digest(spec))}
@@ -119,6 +143,7 @@ def main():
     jobs = {
         "operators": make_operators,
         "random": make_random,
+        "flow": make_flow,
         "acoustic1d": lambda: make_workload("acoustic1d_water.npz",
                                             workloads.acoustic1d_water(), True),
         "axi_small": lambda: make_workload(

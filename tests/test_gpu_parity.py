@@ -276,3 +276,69 @@ def test_tile_menu_parity(gpu, tile, kind, stages, precision, nx):
     assert max_rel_l2_signals(sig, sg_o) <= tol
     for c in st_o:
         assert rel_l2(st[c], st_o[c]) <= tol, c
+
+
+def _flow_cases():
+    g = golden("acoustic_flow.npz")
+    return json.loads(str(g["cases"])), g
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_acoustic_flow_vs_reference(gpu, exact):
+    """AcousticFlow2D: moving-medium row shifts between steps, on the device."""
+    import warnings
+    cases, g = _flow_cases()
+    for case in cases:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            spec = S.flow_scenario(case["seed"], case["nx"], case["ny"], steps=case["steps"],
+                                   flow=case["flow"], mu=case["mu"])
+            prefix = "f%d/" % case["seed"]
+            apply_inputs(spec, g, prefix)
+            f = build_field(spec, exact=exact)
+        f.simulate(spec["steps"])
+        st, sig = field_results(f)
+        comps = O.components_of("AcousticFlow2D")
+        check_state(st, g, prefix, comps, exact)
+        check_signals(sig, g, prefix, comps, exact)
+
+
+def test_acoustic_flow_sim_step_and_apply_flow(gpu):
+    """sim_step loop == simulate; apply_flow alone == the oracle's shift."""
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        spec = S.flow_scenario(41, 130, 20, steps=10, flow="rows")
+        a = build_field(spec)
+        b = build_field(spec)
+    a.simulate(10)
+    for _ in range(10):
+        b.sim_step()
+        b.step += 1
+    sa, ga = field_results(a)
+    sb, gb = field_results(b)
+    for c in sa:
+        assert np.array_equal(sa[c], sb[c])
+        for x, y in zip(ga[c], gb[c]):
+            assert np.array_equal(x, y)
+    # the shift alone, at a step where some rows are due
+    st = {c: np.array(getattr(a, c).values) for c in O.components_of("AcousticFlow2D")}
+    a.step = 12
+    a.apply_flow()
+    O.apply_flow(st, O.flow_periods(spec), 12, spec["nx"])
+    for c in st:
+        assert np.array_equal(np.array(getattr(a, c).values), st[c]), c
+
+
+def test_acoustic_flow_large_grid_vs_oracle(gpu):
+    """A 1000 x 300 flow field (rows of several shift chunks) against the oracle."""
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        spec = S.flow_scenario(43, 1000, 300, steps=8, flow="rows", mu=False)
+        f = build_field(spec, exact=True)
+    f.simulate(8)
+    st, sig = field_results(f)
+    ref_st, ref_sig = O.simulate(spec, 8)
+    for c in st:
+        assert np.array_equal(st[c], ref_st[c]), c

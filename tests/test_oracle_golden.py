@@ -208,3 +208,42 @@ def test_oracle_matches_live_reference():
         b = ref_build.run_reference(spec, spec["steps"])
         for c in a[0]:
             assert np.array_equal(a[0][c], b[0][c])
+
+
+def test_oracle_flow_bitwise():
+    """AcousticFlow2D (pyfds/acoustic_flow.py): the oracle against the reference's
+    trajectories, bit for bit (per-row and scalar flows, periods 1..9, negative
+    periods, a row at rest)."""
+    import warnings
+    from golden_digest import spec_digest
+    from golden_inputs import apply_inputs
+    g = _load("acoustic_flow.npz")
+    for case in json.loads(str(g["cases"])):
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            spec = S.flow_scenario(case["seed"], case["nx"], case["ny"], steps=case["steps"],
+                                   flow=case["flow"], mu=case["mu"])
+        prefix = "f%d/" % case["seed"]
+        apply_inputs(spec, g, prefix)
+        assert str(g[prefix + "digest"]) == spec_digest(spec), "scenario generator drifted"
+        st, sig = O.simulate(spec, spec["steps"])
+        for c in O.components_of("AcousticFlow2D"):
+            assert np.array_equal(st[c], g[prefix + c + "/state"]), (case, c)
+            for j, s in enumerate(sig[c]):
+                assert np.array_equal(s, g[prefix + c + "/sig%d" % j]), (case, c, j)
+
+
+def test_oracle_flow_matches_live_reference():
+    import warnings
+    from oracle import ref_loader
+    if not ref_loader.reference_available():
+        pytest.skip("reference source tree not available")
+    from oracle import ref_build
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for seed in (301, 302):
+            spec = S.flow_scenario(seed, 10, 6, steps=25, flow="rows" if seed % 2 else "scalar")
+            a = O.simulate(spec, spec["steps"])
+            b = ref_build.run_reference(spec, spec["steps"])
+            for c in a[0]:
+                assert np.array_equal(a[0][c], b[0][c])
