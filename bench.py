@@ -1,7 +1,7 @@
 """Benchmark of the pyfds GB300 time-stepping path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload acoustic2d|acoustic1d|axi|thermal|batched|flow]
+                    [--workload acoustic2d|acoustic1d|axi|thermal|batched|flow|nonlinear1d]
                     [--precision f64|f32|f32_t64]
 
 One benchmark step is one full ``simulate()`` of the workload (default: the
@@ -40,10 +40,12 @@ WORKLOADS = {
     "batched": ("layered_media_batch", {}, {"f64": 64, "f32": 32}),
     # the moving-medium shift adds 6 x 8 B per cell every `period` (10) steps
     "flow": ("acoustic_flow_block", {}, {"f64": 64, "f32": 32}),
+    # p, v, rho read + written, 4 coefficient arrays (the whole field stays in L1/L2)
+    "nonlinear1d": ("ideal_gas_column", {}, {"f64": 80}),
 }
 # CPU sample per process and step of the reference arm (time steps), per workload
 CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 10,
-                    "batched": 60, "flow": 20}
+                    "batched": 60, "flow": 20, "nonlinear1d": 400}
 L2_BYTES = 129 * 2 ** 20
 
 
@@ -672,13 +674,17 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": ("stag_step_kernel + flow_shift_kernel + prologue per step"
-                                    if args.workload == "flow" else "stag_step_kernel"),
+                         "kernel": {"flow": "stag_step_kernel + flow_shift_kernel + prologue "
+                                            "per step",
+                                    "nonlinear1d": "nl1d_kernel (every step in one launch; the "
+                                                   "field stays in L1/L2)"}.get(
+                                        args.workload, "stag_step_kernel"),
                          "bytes_per_cell": bpc, "launch_ms": launch_ms},
             "clocks": clk.summary(),
             # per simulate(): a prologue, then per step the step kernel (and, for a
             # moving medium, the row shift and the next step's pressure bounds)
-            "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else nt + 1))}
+            "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else
+                                              1 if args.workload == "nonlinear1d" else nt + 1))}
     if args.time_steps:
         line["config"]["note"] = "time axis shortened for profiling; not a benchmark value"
     if ws == 1 and not args.no_cpu_baseline:

@@ -225,6 +225,41 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps,
                      int32_t store_flux, void* stream);
 
+/* ---------------------------------------------------------------- nonlinear 1-D
+ * IdealGas1D and Acoustic2ndOrder1D (pyfds/nonlinear_acoustics.py:10-171): pressure,
+ * velocity and density on a 1-D grid. One step: pressure bounds/outputs;
+ *   v -= a_v_p p / (rho0 + d) [+ a_v_v2 v] - a_v_v v / (rho0 + d);
+ * velocity bounds/outputs; d -= a_d_v ((d + rho0) v); density bounds/outputs; then
+ * the state equation: ideal gas p = e1 ((rho0 + d) / rho0)^e2 - e1 (nonlinear,
+ * e1 = rho0 c^2 / gamma, e2 = gamma, evaluated as e1 * (x^e2 - 1)) or p = e1 d
+ * (linear, e1 = c^2); second order p = e1 d + e2 d^2 (e1 = d_rho_p, e2 = d_rho2_p / 2). */
+#define FDS_NL1D_IDEAL_GAS 0
+#define FDS_NL1D_SECOND_ORDER 1
+#define FDS_NL1D_CONVECTIVE 1u /* the central a_v_v2 term (always on for second order) */
+#define FDS_NL1D_NL_STATE 2u   /* ideal gas: nonlinear state equation */
+
+typedef struct FdsNl1dProblem {
+  int32_t kind;      /* FDS_NL1D_* */
+  uint32_t flags;    /* FDS_NL1D_CONVECTIVE | FDS_NL1D_NL_STATE | FDS_FLAG_EXACT */
+  int32_t n;         /* cells */
+  int32_t tile_x;    /* tiling the boundary/output tables were bucketed for */
+  double f1;         /* dt/dx: the diagonals of a_v_p (backward) and a_d_v (forward) */
+  double fc;         /* (dt/dx/2)/2: the diagonals of the central a_v_v2 */
+  const double* a;   /* [n] dt/dx^2 mu: the a_v_v diagonals (a, -2a, a) */
+  const double* rho0;/* [n] static density */
+  const double* e1;  /* [n] state-equation factor (see above) */
+  const double* e2;  /* [n] state-equation factor or exponent (see above) */
+} FdsNl1dProblem;
+
+/* Advances a nonlinear 1-D field by nsteps steps in one launch (one CTA loops over
+ * the steps; the grid is small). state->cur/nxt: pressure (updated in place in cur),
+ * velocity and density (ping-pong, swapped per step like fds_stag_run). tables->comp:
+ * pressure, velocity, density. Replaces the loop of Field.simulate around
+ * IdealGas1D.sim_step / Acoustic2ndOrder1D.sim_step (pyfds/nonlinear_acoustics.py:55-90,
+ * 140-163). */
+int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* state,
+                     const FdsStagTables* tables, int64_t step0, int32_t nsteps, void* stream);
+
 /* The moving-medium shift of one step alone, in place on state->cur (p, vx, vy):
  * replaces AcousticFlow2D.apply_flow (pyfds/acoustic_flow.py:49-57) for callers that
  * step a flow field themselves. Needs FDS_FLAG_FLOW and flow_period. */

@@ -189,6 +189,8 @@ def components_of(kind):
         "AcousticFlow2D": ["pressure", "velocity_x", "velocity_y"],
         "Acoustic3DAxi": ["pressure", "velocity_x", "velocity_y"],
         "Thermal1D": ["temperature", "heat_flux"],
+        "IdealGas1D": ["pressure", "velocity", "density"],
+        "Acoustic2ndOrder1D": ["pressure", "velocity", "density"],
         "Thermal2D": ["temperature", "heat_flux_x", "heat_flux_y"],
         "Thermal3DAxi": ["temperature", "heat_flux_x", "heat_flux_y"],
     }[kind]
@@ -219,6 +221,23 @@ def assemble(spec):
     ops = {"n": n, "nx": nx}
     if kind == "AcousticFlow2D":
         kind = "Acoustic2D"  # pyfds/acoustic_flow.py:13: the Acoustic2D operators
+    if kind in ("IdealGas1D", "Acoustic2ndOrder1D"):
+        # pyfds/nonlinear_acoustics.py:38-53 and :124-138
+        ops["a_d_v"] = d_x(n, dt / dx * np.ones(nx))
+        ops["a_v_p"] = d_x(n, (dt / dx) * np.ones(nx), variant="backward")
+        ops["a_v_v"] = d_x2(n, dt / dx ** 2 * mv("absorption_coef"))
+        ops["a_v_v2"] = d_x(n, (dt / dx / 2) * np.ones(nx), variant="central")
+        ops["stat_density"] = mv("density")
+        if kind == "IdealGas1D":
+            ops["sound_velocity"] = mv("sound_velocity")
+            ops["heat_cap_ratio"] = mv("isobaric_heat_cap") / mv("isochoric_heat_cap")
+            ops["convective"] = bool(spec.get("convective", True))
+            ops["nl_state"] = bool(spec.get("nl_state", True))
+        else:
+            ops["d_rho_p"] = mv("d_rho_p")
+            ops["d_rho2_p"] = mv("d_rho2_p")
+            ops["convective"] = True
+        return ops
     if kind == "Acoustic1D":
         # pyfds/acoustics.py:27-38
         ops["a_p_v"] = d_x(n, dt / dx * mv("sound_velocity") ** 2 * mv("density"))
@@ -321,7 +340,32 @@ def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
         apply_bounds(state[name], bounds.get(name, []), step)
         write_outputs(state[name], outputs.get(name, []), signals.setdefault(name, []))
 
-    if kind == "Acoustic1D":
+    if kind in ("IdealGas1D", "Acoustic2ndOrder1D"):
+        # pyfds/nonlinear_acoustics.py:55-90 and :140-163
+        pre("pressure")
+        rho0 = ops["stat_density"]
+        v = state["velocity"]
+        if ops["convective"]:
+            state["velocity"] = v - (mv(ops["a_v_p"], state["pressure"]) / (rho0 + state["density"])
+                                     + mv(ops["a_v_v2"], v)
+                                     - mv(ops["a_v_v"], v) / (rho0 + state["density"]))
+        else:
+            state["velocity"] = v - (mv(ops["a_v_p"], state["pressure"]) / (rho0 + state["density"])
+                                     - mv(ops["a_v_v"], v) / (rho0 + state["density"]))
+        pre("velocity")
+        state["density"] = state["density"] - mv(ops["a_d_v"],
+                                                 (state["density"] + rho0) * state["velocity"])
+        pre("density")
+        d = state["density"]
+        if kind == "IdealGas1D":
+            c, g = ops["sound_velocity"], ops["heat_cap_ratio"]
+            if ops["nl_state"]:
+                state["pressure"] = rho0 * c ** 2 / g * (((rho0 + d) / rho0) ** g - 1)
+            else:
+                state["pressure"] = c ** 2 * d
+        else:
+            state["pressure"] = ops["d_rho_p"] * d + ops["d_rho2_p"] / 2 * d ** 2
+    elif kind == "Acoustic1D":
         # pyfds/acoustics.py:40-52
         pre("pressure")
         state["velocity"] = state["velocity"] - (mv(ops["a_v_p"], state["pressure"])

@@ -15,7 +15,7 @@ from .ref_loader import load_reference
 
 
 def _make_material(pyfds, kind, params):
-    if kind.startswith("Acoustic"):
+    if kind.startswith("Acoustic") or kind == "IdealGas1D":
         p = dict(params)
         mat = pyfds.AcousticMaterial(p.pop("sound_velocity"), p.pop("density"))
         for k, v in p.items():
@@ -37,7 +37,11 @@ def build_reference_field(spec):
     mats = spec["materials"]
     assert mats[0][0] is None, "first material must be the main material"
     main = _make_material(pyfds, kind, mats[0][1])
-    if kind.endswith("1D"):
+    if kind == "IdealGas1D":
+        fld = cls(spec.get("convective", True), spec.get("nl_state", True),
+                  x_samples=spec["nx"], x_delta=spec["dx"], t_samples=spec["nt"],
+                  t_delta=spec["dt"], material=main)
+    elif kind.endswith("1D"):
         fld = cls(x_samples=spec["nx"], x_delta=spec["dx"], t_samples=spec["nt"],
                   t_delta=spec["dt"], material=main)
     else:

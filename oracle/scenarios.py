@@ -144,3 +144,53 @@ def flow_scenario(seed, nx, ny, steps=60, flow="rows", mu=True):
         v[rng.integers(0, ny)] = 0.0
         spec["flow"] = v
     return spec
+
+
+def nonlinear_scenario(seed, kind, nx, steps=60, convective=True, nl_state=True, mu=True):
+    """A random 1-D nonlinear acoustic scenario (``IdealGas1D`` or
+    ``Acoustic2ndOrder1D``, pyfds/nonlinear_acoustics.py): a gas (or liquid) with
+    1..2 extra material regions, a small random initial density perturbation, a
+    pressure source cell driven by a pulse, velocity held at 0 at both ends, and
+    outputs on every component."""
+    rng = np.random.default_rng(seed)
+    dx = 1e-3
+    liquid = kind == "Acoustic2ndOrder1D"
+
+    def material():
+        c = float(rng.uniform(1400, 1600) if liquid else rng.uniform(300, 360))
+        rho = float(rng.uniform(900, 1100) if liquid else rng.uniform(1.0, 1.4))
+        p = {"sound_velocity": c, "density": rho,
+             "absorption_coef": float(rng.uniform(1e-4, 1e-2) * rho * c * dx) if mu else 0,
+             "isobaric_heat_cap": float(rng.uniform(1.3, 1.7)), "isochoric_heat_cap": 1.0}
+        if liquid:
+            p["d_rho_p"] = c * c
+            p["d_rho2_p"] = float(rng.uniform(1e6, 1e7))
+        return p
+
+    mats = [(None, material())]
+    for _ in range(int(rng.integers(1, 3))):
+        a, b = sorted(rng.integers(0, nx, size=2))
+        mats.append((np.arange(a, b + 1), material()))
+    cmax = max(m[1]["sound_velocity"] for m in mats)
+    dt = 0.4 * dx / cmax
+    rho0 = mats[0][1]["density"]
+    # weak enough to stay finite over a few hundred steps (the reference's central
+    # convective term grows slowly with forward Euler stepping)
+    rel = 1e-5 if liquid else 1e-3
+    init = {"density": rng.standard_normal(nx) * rel * rho0}
+    t = np.arange(steps) * dt
+    f0 = cmax / (12 * dx)
+    amp = 10 * rel * rho0 * cmax ** 2
+    src = int(rng.integers(1, nx - 1))
+    spec = {"kind": kind, "nx": nx, "dx": dx, "dt": dt, "nt": steps, "steps": steps,
+            "materials": mats, "init": init,
+            "bounds": {"pressure": [{"indices": [src], "value": _pulse(t, f0, 4 / f0, 1 / f0, amp),
+                                     "additive": False}],
+                       "velocity": [{"indices": [0, nx - 1], "value": 0.0, "additive": False}]},
+            "outputs": {"pressure": [[src, int(rng.integers(0, nx))]],
+                        "velocity": [[int(rng.integers(0, nx)), int(rng.integers(0, nx))]],
+                        "density": [[int(rng.integers(0, nx))]]}}
+    if kind == "IdealGas1D":
+        spec["convective"] = bool(convective)
+        spec["nl_state"] = bool(nl_state)
+    return spec

@@ -34,12 +34,18 @@ FLAG_AXI = 4
 FLAG_EXACT = 8
 FLAG_FLOW = 16
 
+NL1D_IDEAL_GAS = 0
+NL1D_SECOND_ORDER = 1
+NL1D_CONVECTIVE = 1
+NL1D_NL_STATE = 2
+
 BOP_SIGNAL = 2
 
 # exported symbols, in header order
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
                     "fds_stag_batch_run", "fds_stag_batch_run_static", "fds_stag_flow_shift",
+                    "fds_nl1d_run",
                     # include/fds_surrogate.h
                     "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
                     "fds_conv_wgrad_max_grid", "fds_adamw", "fds_surr_pack", "fds_surr_loss",
@@ -95,6 +101,12 @@ PROBE_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("col", "<i4")], align=
 assert BOUND_OP_DTYPE.itemsize == 32
 assert BOUND_GROUP_DTYPE.itemsize == 24
 assert PROBE_DTYPE.itemsize == 16
+
+
+class FdsNl1dProblem(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("flags", C.c_uint32), ("n", C.c_int32),
+                ("tile_x", C.c_int32), ("f1", C.c_double), ("fc", C.c_double),
+                ("a", C.c_void_p), ("rho0", C.c_void_p), ("e1", C.c_void_p), ("e2", C.c_void_p)]
 
 
 class FdsConvArgs(C.Structure):
@@ -181,9 +193,15 @@ def load(path=None):
     lib.fds_stag_batch_run_static.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                               C.POINTER(FdsStagTables), C.c_int32, C.c_int64,
                                               C.c_int32, C.c_int32, C.c_void_p]
+    lib.fds_nl1d_run.restype = C.c_int32
+    lib.fds_nl1d_run.argtypes = [C.POINTER(FdsNl1dProblem), C.POINTER(FdsStagState),
+                                 C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_void_p]
     lib.fds_stag_flow_shift.restype = C.c_int32
     lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                         C.c_int64, C.c_void_p]
+    lib.fds_nl1d_run.restype = C.c_int32
+    lib.fds_nl1d_run.argtypes = [C.POINTER(FdsNl1dProblem), C.POINTER(FdsStagState),
+                                 C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_void_p]
     lib.fds_stag_flow_shift.restype = C.c_int32
     lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                         C.c_int64, C.c_void_p]

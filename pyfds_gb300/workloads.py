@@ -13,7 +13,7 @@ field; the same spec drives the CPU oracle in the tests.
 """
 import numpy as np
 
-from . import acoustic_flow, acoustics, regions as reg, thermal
+from . import acoustic_flow, acoustics, nonlinear_acoustics, regions as reg, thermal
 
 WATER = {"sound_velocity": 1500.0, "density": 1000.0, "absorption_coef": 0}
 STEEL = {"sound_velocity": 5900.0, "density": 7850.0, "absorption_coef": 0}
@@ -83,6 +83,27 @@ def acoustic_flow_block(n=2048, nt=4000, n_probes=64, seed=2, period=10):
     spec["kind"] = "AcousticFlow2D"
     spec["flow"] = float(spec["dx"] / (period + 0.5) / spec["dt"])
     return spec
+
+
+def ideal_gas_column(n=1000, nt=20000, nl_state=True):
+    """IdealGas1D: a 1 m air column (c = 343 m/s, rho = 1.2 kg/m^3, gamma = 1.4,
+    light absorption), dx = 1 mm, dt at CFL 0.5; a finite-amplitude 10 kPa pressure
+    pulse (5 kHz, Gaussian-modulated) driven at cell 1, velocity 0 at both ends,
+    pressure outputs at the quarter points."""
+    dx = 1e-3
+    c, rho = 343.0, 1.2
+    dt = 0.5 * dx / c
+    t = np.arange(nt) * dt
+    mat = {"sound_velocity": c, "density": rho, "absorption_coef": 1.8e-5,
+           "isobaric_heat_cap": 1.4, "isochoric_heat_cap": 1.0}
+    return {"kind": "IdealGas1D", "nx": n, "dx": dx, "dt": dt, "nt": nt, "steps": nt,
+            "convective": True, "nl_state": nl_state,
+            "materials": [(None, mat)],
+            "bounds": {"pressure": [{"indices": [1],
+                                     "value": gauss_pulse(t, 5e3, 4e-4, 1e-4, 1e4),
+                                     "additive": False}],
+                       "velocity": [{"indices": [0, n - 1], "value": 0.0, "additive": False}]},
+            "outputs": {"pressure": [[n // 4, n // 2, 3 * n // 4]]}}
 
 
 def axi_disc_source(nr=1024, nz=4096, nt=6000, disc=200, probe_every=64):
@@ -233,7 +254,7 @@ def surrogate_media(count, seed, n=256, nt=4096, t_src=704):
 
 def _material(kind, params):
     p = dict(params)
-    if kind.startswith("Acoustic"):
+    if kind.startswith("Acoustic") or kind == "IdealGas1D":
         mat = acoustics.AcousticMaterial(p.pop("sound_velocity"), p.pop("density"))
         for k, v in p.items():
             setattr(mat, k, v)
@@ -248,9 +269,12 @@ def build_field(spec, **kwargs):
     constructor, e.g. ``precision`` or ``exact``)."""
     kind = spec["kind"]
     cls = (getattr(acoustics, kind, None) or getattr(acoustic_flow, kind, None)
-           or getattr(thermal, kind))
+           or getattr(nonlinear_acoustics, kind, None) or getattr(thermal, kind))
     mats = spec["materials"]
     main = _material(kind, mats[0][1])
+    if kind == "IdealGas1D":
+        kwargs = dict(kwargs, convective=spec.get("convective", True),
+                      nl_state=spec.get("nl_state", True))
     if kind.endswith("1D"):
         f = cls(x_samples=spec["nx"], x_delta=spec["dx"], t_samples=spec["nt"],
                 t_delta=spec["dt"], material=main, **kwargs)

@@ -22,6 +22,9 @@ source is not modified. Fixtures:
   and thermal workloads for their first 100 steps (--skip-large skips them).
 - acoustic_flow.npz: AcousticFlow2D (moving medium) scenarios, oracle/scenarios.py
   ``flow_scenario``: per-row and scalar flows, periods 1..9, negative and zero flows.
+- nonlinear_1d.npz: IdealGas1D (convective or not, nonlinear or linear state
+  equation) and Acoustic2ndOrder1D scenarios, oracle/scenarios.py
+  ``nonlinear_scenario``.
 """
 import argparse
 import json
@@ -58,6 +61,15 @@ FLOW_CASES = [{"seed": 200 + k, "nx": nx, "ny": ny, "steps": 45, "flow": fl, "mu
                                                     (7, 11, "scalar", True), (33, 4, "rows", True),
                                                     (5, 9, "scalar", False), (12, 12, "rows", False),
                                                     (64, 3, "rows", True)])]
+
+
+NL_CASES = [{"seed": 400 + k, "kind": kind, "nx": nx, "steps": 120, "convective": conv,
+             "nl_state": nls, "mu": mu}
+            for k, (kind, nx, conv, nls, mu) in enumerate([
+                ("IdealGas1D", 40, True, True, True), ("IdealGas1D", 97, False, True, True),
+                ("IdealGas1D", 64, True, False, False), ("IdealGas1D", 1500, True, True, True),
+                ("Acoustic2ndOrder1D", 50, True, True, True),
+                ("Acoustic2ndOrder1D", 1200, True, True, False)])]
 
 
 def run_and_pack(spec, prefix, out, keep_state=True, steps=None, materials=False):
@@ -127,6 +139,19 @@ def make_flow():
     np.savez_compressed(os.path.join(HERE, "acoustic_flow.npz"), **out)
 
 
+def make_nonlinear():
+    out = {}
+    for case in NL_CASES:
+        spec = scenarios.nonlinear_scenario(case["seed"], case["kind"], case["nx"],
+                                            steps=case["steps"], convective=case["convective"],
+                                            nl_state=case["nl_state"], mu=case["mu"])
+        prefix = "n%d/" % case["seed"]
+        out[prefix + "digest"] = np.array(spec_digest(spec))
+        run_and_pack(spec, prefix, out, materials=True)
+    out["cases"] = np.array(json.dumps(NL_CASES))
+    np.savez_compressed(os.path.join(HERE, "nonlinear_1d.npz"), **out)
+
+
 def make_workload(name, spec, keep_state, steps=None):
     t0 = time.time()
     out = {"digest": np.array(spec_digest(spec))}
@@ -144,6 +169,7 @@ def main():
         "operators": make_operators,
         "random": make_random,
         "flow": make_flow,
+        "nonlinear": make_nonlinear,
         "acoustic1d": lambda: make_workload("acoustic1d_water.npz",
                                             workloads.acoustic1d_water(), True),
         "axi_small": lambda: make_workload(

@@ -342,3 +342,41 @@ def test_acoustic_flow_large_grid_vs_oracle(gpu):
     ref_st, ref_sig = O.simulate(spec, 8)
     for c in st:
         assert np.array_equal(st[c], ref_st[c]), c
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_nonlinear_1d_vs_reference(gpu, exact):
+    """IdealGas1D / Acoustic2ndOrder1D in one launch per simulate() call. Exact mode
+    is bit-identical except where the ideal-gas state equation calls pow (device and
+    host libm may differ in the last bit): there the 1e-12 bar applies."""
+    g = golden("nonlinear_1d.npz")
+    for case in json.loads(str(g["cases"])):
+        spec = S.nonlinear_scenario(case["seed"], case["kind"], case["nx"], steps=case["steps"],
+                                    convective=case["convective"], nl_state=case["nl_state"],
+                                    mu=case["mu"])
+        prefix = "n%d/" % case["seed"]
+        apply_inputs(spec, g, prefix)
+        f = build_field(spec, exact=exact)
+        f.simulate(spec["steps"])
+        assert f.step == spec["steps"]
+        st, sig = field_results(f)
+        comps = O.components_of(case["kind"])
+        bitwise = exact and not (case["kind"] == "IdealGas1D" and case["nl_state"])
+        check_state(st, g, prefix, comps, bitwise)
+        check_signals(sig, g, prefix, comps, bitwise)
+
+
+def test_nonlinear_1d_sim_step_loop_equals_simulate(gpu):
+    spec = S.nonlinear_scenario(77, "Acoustic2ndOrder1D", 300, steps=25)
+    a = build_field(spec)
+    a.simulate(25)
+    b = build_field(spec)
+    for _ in range(25):
+        b.sim_step()
+        b.step += 1
+    sa, ga = field_results(a)
+    sb, gb = field_results(b)
+    for c in sa:
+        assert np.array_equal(sa[c], sb[c])
+        for x, y in zip(ga[c], gb[c]):
+            assert np.array_equal(x, y)

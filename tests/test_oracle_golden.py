@@ -247,3 +247,27 @@ def test_oracle_flow_matches_live_reference():
             b = ref_build.run_reference(spec, spec["steps"])
             for c in a[0]:
                 assert np.array_equal(a[0][c], b[0][c])
+
+
+def _nl_spec(case):
+    return S.nonlinear_scenario(case["seed"], case["kind"], case["nx"], steps=case["steps"],
+                                convective=case["convective"], nl_state=case["nl_state"],
+                                mu=case["mu"])
+
+
+def test_oracle_nonlinear_bitwise():
+    """IdealGas1D / Acoustic2ndOrder1D (pyfds/nonlinear_acoustics.py): the oracle
+    against the reference's trajectories, bit for bit."""
+    from golden_digest import spec_digest
+    from golden_inputs import apply_inputs
+    g = _load("nonlinear_1d.npz")
+    for case in json.loads(str(g["cases"])):
+        spec = _nl_spec(case)
+        prefix = "n%d/" % case["seed"]
+        apply_inputs(spec, g, prefix)
+        assert str(g[prefix + "digest"]) == spec_digest(spec), "scenario generator drifted"
+        st, sig = O.simulate(spec, spec["steps"])
+        for c in O.components_of(case["kind"]):
+            assert np.array_equal(st[c], g[prefix + c + "/state"]), (case, c)
+            for j, s in enumerate(sig[c]):
+                assert np.array_equal(s, g[prefix + c + "/sig%d" % j]), (case, c, j)
