@@ -201,7 +201,7 @@ def _radii(nx, ny, dx):
     return np.tile(np.arange(0, nx) * dx, ny) + dx / 2
 
 
-def assemble(spec):
+def assemble(spec, scale=None):
     """Build the operators of one field (the ``assemble_matrices`` of each kind).
 
     ``spec`` keys: kind, nx, ny (2-D), dx, dy (2-D), dt, materials.
@@ -216,6 +216,10 @@ def assemble(spec):
     mats = spec["materials"]
 
     def mv(name):
+        # a MaterialCoupling multiplies one parameter by its transfer factors
+        # (pyfds/coupling.py:181-196)
+        if scale and name in scale:
+            return material_vector(n, mats, name) * scale[name]
         return material_vector(n, mats, name)
 
     ops = {"n": n, "nx": nx}
@@ -485,3 +489,121 @@ def simulate(spec, num_steps=None, state=None, step0=0):
     out = {c: [np.array(sig, dtype=np.float64).reshape(len(sig), -1) for sig in signals[c]]
            for c in signals}
     return state, out
+
+
+# --------------------------------------------------------------------------------------
+# Coupled fields (pyfds/coupling.py, pyfds/coupled_fields.py)
+# --------------------------------------------------------------------------------------
+
+
+def transfer(fn, values):
+    """Transfer functions of the coupling scenarios: ("quad", c) -> c x^2,
+    ("power", power, factor) -> 1 + factor x^power (pyfds/coupling.py:287-300),
+    ("exp", a, b) -> a + (1 - a) exp(b x) (pyfds/coupling.py:243-254)."""
+    if fn[0] == "quad":
+        return fn[1] * values ** 2
+    if fn[0] == "power":
+        return 1 + fn[2] * values ** fn[1]
+    if fn[0] == "exp":
+        return fn[1] + (1 - fn[1]) * np.exp(fn[2] * values)
+    raise ValueError(fn)
+
+
+def thermoacoustic_spec_fields(spec):
+    """The two field specs of ThermoAcoustic1D (pyfds/coupled_fields.py:18-39)."""
+    base = {"nx": spec["nx"], "dx": spec["dx"], "dt": spec["dt"], "nt": spec["nt"]}
+    ac = dict(base, kind="Acoustic1D", materials=[(None, spec["acoustic_material"])])
+    th = dict(base, kind="Thermal1D", materials=[(None, spec["thermal_material"])])
+    for f, names in ((ac, ("pressure", "velocity")), (th, ("temperature", "heat_flux"))):
+        for key in ("bounds", "outputs", "init"):
+            sub = {c: v for c, v in (spec.get(key) or {}).items() if c in names}
+            if sub:
+                f[key] = sub
+    return [ac, th]
+
+
+def coupled_interactions(spec):
+    """Interaction list of a coupled spec; ThermoAcoustic1D's loss coupling is
+    ("loss") from the acoustic velocity into the temperature."""
+    if spec["kind"] == "ThermoAcoustic1D":
+        st = spec.get("stepping", 1)
+        return [{"type": "boundary", "src": [0, "velocity"], "dst": [1, "temperature"],
+                 "fn": ["loss"], "additive": True, "accumulate": st > 1, "stepping": st}]
+    return spec["interactions"]
+
+
+def simulate_coupled(spec, num_steps=None):
+    """``SynchronizedFields.simulate`` (pyfds/coupling.py:14-87 with
+    pyfds/fields.py:67-95): assemble every field (material couplings apply their
+    factors of the initial source values), then per step every field's sim_step in
+    list order and every interaction's apply(step). Returns ([(state, signals) per
+    field])."""
+    fields = (thermoacoustic_spec_fields(spec) if spec["kind"] == "ThermoAcoustic1D"
+              else spec["fields"])
+    inter = coupled_interactions(spec)
+    n = fields[0]["nx"] * fields[0].get("ny", 1)
+    states = []
+    for f in fields:
+        st = {c: np.zeros(n) for c in components_of(f["kind"])}
+        for c, v in (f.get("init") or {}).items():
+            st[c] = np.array(v, dtype=np.float64).copy()
+        states.append(st)
+    scales = [dict() for _ in fields]
+
+    def mat_factors(it):
+        return transfer(it["fn"], states[it["src"][0]][it["src"][1]])
+
+    for it in inter:
+        if it["type"] == "material":
+            scales[it["field"]][it["param"]] = mat_factors(it)
+            it["_last"] = 0
+    ops = [assemble(f, scales[k]) for k, f in enumerate(fields)]
+    signals = []
+    for f in fields:
+        outs = f.get("outputs") or {}
+        signals.append({c: [[[] for _ in idx] for idx in outs.get(c, [])]
+                        for c in components_of(f["kind"])})
+    acc = [0 for _ in inter]
+    if num_steps is None:
+        num_steps = spec["nt"]
+    for s in range(num_steps):
+        for k, f in enumerate(fields):
+            sim_step(f["kind"], ops[k], states[k], f.get("bounds") or {}, f.get("outputs") or {},
+                     signals[k], s, dt=f["dt"])
+        for j, it in enumerate(inter):
+            if it["type"] == "boundary":
+                src = states[it["src"][0]][it["src"][1]]
+                if it["fn"][0] == "loss":
+                    # ThermoAcoustic1D._loss_coupling (pyfds/coupled_fields.py:45-65)
+                    ac_f, th_f = fields
+                    vd = dia_matvec(ops[0]["a_v_p"], src * material_vector(n, ac_f["materials"],
+                                                                            "density"))
+                    tf = lambda: (material_vector(n, ac_f["materials"], "absorption_coef")
+                                  / material_vector(n, th_f["materials"], "density")
+                                  / material_vector(n, th_f["materials"], "heat_capacity")
+                                  * vd ** 2 * spec["dt"])
+                else:
+                    tf = lambda: transfer(it["fn"], src)
+                dst = states[it["dst"][0]]
+                name = it["dst"][1]
+                if it["accumulate"] is True:
+                    acc[j] += tf()
+                if s % it["stepping"] == 0:
+                    val = tf() if it["accumulate"] is False else acc[j]
+                    if it["accumulate"] is not False:
+                        acc[j] = 0
+                    dst[name] = dst[name] + val if it["additive"] is True else val
+            elif it["type"] == "material":
+                if s % it["stepping"] == 0:
+                    tf = mat_factors(it)
+                    rel = max(abs((tf - it["_last"]) / tf))
+                    if it.get("rel") is None or rel > it["rel"]:
+                        scales[it["field"]][it["param"]] = tf
+                        ops[it["field"]] = assemble(fields[it["field"]], scales[it["field"]])
+                        it["_last"] = tf
+    out = []
+    for k, f in enumerate(fields):
+        sig = {c: [np.array(x, dtype=np.float64).reshape(len(x), -1) for x in signals[k][c]]
+               for c in signals[k]}
+        out.append((states[k], sig))
+    return out

@@ -194,3 +194,138 @@ def nonlinear_scenario(seed, kind, nx, steps=60, convective=True, nl_state=True,
         spec["convective"] = bool(convective)
         spec["nl_state"] = bool(nl_state)
     return spec
+
+
+# ------------------------------------------------------------------ coupled fields
+
+def coupled_scenario(seed, variant, nx=30, steps=40):
+    """Coupled 1-D scenarios (pyfds/coupling.py, pyfds/coupled_fields.py):
+
+    - "thermoacoustic" / "thermoacoustic3": ThermoAcoustic1D with a driven pressure
+      cell (stepping 1, or 3 with accumulation);
+    - "sync": Acoustic1D + Thermal1D in SynchronizedFields with a quadratic
+      BoundaryCoupling of the pressure into the temperature (stepping 2, accumulated)
+      and a power-law MaterialCoupling of the temperature into the sound velocity;
+    - "sync_exp": the same with an exponential MaterialCoupling of the pressure into
+      the thermal conductivity (change threshold 1e-9).
+    """
+    rng = np.random.default_rng(seed)
+    dx = 1e-4
+    ac_mat = {"sound_velocity": float(rng.uniform(1400, 1600)),
+              "density": float(rng.uniform(900, 1100)),
+              "absorption_coef": float(rng.uniform(1e-3, 1e-2))}
+    th_mat = {"heat_capacity": float(rng.uniform(3000, 4500)),
+              "density": float(rng.uniform(900, 1100)),
+              "thermal_conductivity_x": float(rng.uniform(0.4, 0.7))}
+    dt = 0.4 * dx / ac_mat["sound_velocity"]
+    t = np.arange(steps) * dt
+    f0 = ac_mat["sound_velocity"] / (10 * dx)
+    src = int(rng.integers(1, nx - 1))
+    bounds = {"pressure": [{"indices": [src], "value": _pulse(t, f0, 3 / f0, 1 / f0, 1e5),
+                            "additive": True},
+                           {"indices": [0, nx - 1], "value": 0.0, "additive": False}],
+              "temperature": [{"indices": [0], "value": 293.15, "additive": False}]}
+    outputs = {"pressure": [[int(rng.integers(0, nx)), src]],
+               "velocity": [[int(rng.integers(0, nx))]],
+               "temperature": [[int(rng.integers(0, nx)), src]]}
+    init = {"temperature": 293.15 + rng.standard_normal(nx) * 0.01}
+    if variant.startswith("thermoacoustic"):
+        return {"kind": "ThermoAcoustic1D", "nx": nx, "dx": dx, "dt": dt, "nt": steps,
+                "steps": steps, "acoustic_material": ac_mat, "thermal_material": th_mat,
+                "stepping": 3 if variant == "thermoacoustic3" else 1,
+                "bounds": bounds, "outputs": outputs, "init": init}
+    base = {"nx": nx, "dx": dx, "dt": dt, "nt": steps}
+    ac = dict(base, kind="Acoustic1D", materials=[(None, ac_mat)],
+              bounds={"pressure": bounds["pressure"]},
+              outputs={"pressure": outputs["pressure"], "velocity": outputs["velocity"]})
+    th = dict(base, kind="Thermal1D", materials=[(None, th_mat)],
+              bounds={"temperature": bounds["temperature"]},
+              outputs={"temperature": outputs["temperature"]}, init=init)
+    inter = [{"type": "boundary", "src": [0, "pressure"], "dst": [1, "temperature"],
+              "fn": ["quad", 1e-12], "additive": True, "accumulate": True, "stepping": 2}]
+    if variant == "sync":
+        inter.append({"type": "material", "src": [1, "temperature"], "field": 0,
+                      "param": "sound_velocity", "fn": ["power", 1, 1e-4], "rel": None,
+                      "stepping": 2})
+    else:
+        inter.append({"type": "material", "src": [0, "pressure"], "field": 1,
+                      "param": "thermal_conductivity_x", "fn": ["exp", 0.5, 1e-6],
+                      "rel": 1e-9, "stepping": 1})
+    return {"kind": "Synchronized", "nx": nx, "dt": dt, "nt": steps, "steps": steps,
+            "fields": [ac, th], "interactions": inter}
+
+
+def build_coupled(mod, spec, build_field, **field_kwargs):
+    """The coupled object of ``spec`` from module ``mod`` (the reference package or
+    pyfds_gb300): fields from ``build_field(field_spec)``, interactions from the
+    library's coupling classes."""
+    from .fds_oracle import transfer
+    if spec["kind"] == "ThermoAcoustic1D":
+        def mat(cls, p):
+            p = dict(p)
+            if cls is mod.AcousticMaterial:
+                m = mod.AcousticMaterial(p.pop("sound_velocity"), p.pop("density"))
+                for k, v in p.items():
+                    setattr(m, k, v)
+                return m
+            return mod.ThermalMaterial(p["heat_capacity"], p["density"],
+                                       p["thermal_conductivity_x"])
+        obj = mod.ThermoAcoustic1D(spec["nx"], spec["dx"], spec["nt"], spec["dt"],
+                                   mat(mod.ThermalMaterial, spec["thermal_material"]),
+                                   mat(mod.AcousticMaterial, spec["acoustic_material"]),
+                                   spec.get("stepping", 1), **field_kwargs)
+        for name, v in (spec.get("init") or {}).items():
+            getattr(obj, name).values = np.array(v, dtype=np.float64).copy()
+        regmod = mod.regions
+        for name, blist in (spec.get("bounds") or {}).items():
+            for b in blist:
+                getattr(obj, name).boundaries.append(regmod.Boundary(
+                    regmod.Region(list(map(int, b["indices"])), "boundary"), value=b["value"],
+                    additive=b.get("additive", False)))
+        for name, olist in (spec.get("outputs") or {}).items():
+            for idx in olist:
+                getattr(obj, name).outputs.append(regmod.Output(
+                    regmod.Region(list(map(int, idx)), "output")))
+        return obj
+    fields = [build_field(f, **field_kwargs) for f in spec["fields"]]
+    inter = []
+    for it in spec["interactions"]:
+        if it["type"] == "boundary":
+            fn = it["fn"]
+            inter.append(mod.BoundaryCoupling(
+                getattr(fields[it["src"][0]], it["src"][1]),
+                getattr(fields[it["dst"][0]], it["dst"][1]),
+                lambda x, fn=fn: transfer(fn, x), additive=it["additive"],
+                accumulate=it["accumulate"], stepping=it["stepping"]))
+        else:
+            src = getattr(fields[it["src"][0]], it["src"][1])
+            tgt = fields[it["field"]]
+            fn = it["fn"]
+            if fn[0] == "power":
+                inter.append(mod.MaterialCouplingPowerLaw(src, tgt, it["param"], fn[1], fn[2],
+                                                          rel_change_threshold=it["rel"],
+                                                          stepping=it["stepping"]))
+            elif fn[0] == "exp":
+                inter.append(mod.MaterialCouplingExponential(src, tgt, it["param"], fn[1], fn[2],
+                                                             rel_change_threshold=it["rel"],
+                                                             stepping=it["stepping"]))
+            else:
+                inter.append(mod.MaterialCoupling(src, tgt, it["param"],
+                                                  lambda x, fn=fn: transfer(fn, x),
+                                                  rel_change_threshold=it["rel"],
+                                                  stepping=it["stepping"]))
+    return mod.SynchronizedFields(fields, inter)
+
+
+def coupled_results(obj, kind_of):
+    """([(state, signals)] per field) of a simulated coupled object."""
+    out = []
+    for f in obj.fields:
+        kind = kind_of(f)
+        from .fds_oracle import components_of
+        st = {c: np.array(getattr(f, c).values, dtype=np.float64) for c in components_of(kind)}
+        sig = {c: [np.array(o.signals, dtype=np.float64).reshape(
+            len(np.asarray(o.region.indices).reshape(-1)), -1) for o in getattr(f, c).outputs]
+            for c in components_of(kind)}
+        out.append((st, sig))
+    return out

@@ -8,6 +8,8 @@ regions keep their constructors and attributes, while ``simulate()`` and
 from . import fields, gfx, regions  # noqa: F401
 from .acoustic_flow import *  # noqa: F401,F403
 from .acoustics import *  # noqa: F401,F403
+from .coupled_fields import *  # noqa: F401,F403
+from .coupling import *  # noqa: F401,F403
 from .gfx import *  # noqa: F401,F403
 from .nonlinear_acoustics import *  # noqa: F401,F403
 from .regions import *  # noqa: F401,F403

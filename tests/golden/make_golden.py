@@ -22,6 +22,9 @@ source is not modified. Fixtures:
   and thermal workloads for their first 100 steps (--skip-large skips them).
 - acoustic_flow.npz: AcousticFlow2D (moving medium) scenarios, oracle/scenarios.py
   ``flow_scenario``: per-row and scalar flows, periods 1..9, negative and zero flows.
+- coupling.npz: coupled fields (ThermoAcoustic1D with stepping 1 and 3,
+  SynchronizedFields with boundary and material couplings), oracle/scenarios.py
+  ``coupled_scenario``; inputs stored per field.
 - nonlinear_1d.npz: IdealGas1D (convective or not, nonlinear or linear state
   equation) and Acoustic2ndOrder1D scenarios, oracle/scenarios.py
   ``nonlinear_scenario``.
@@ -152,6 +155,38 @@ def make_nonlinear():
     np.savez_compressed(os.path.join(HERE, "nonlinear_1d.npz"), **out)
 
 
+CPL_CASES = [{"seed": 500 + k, "variant": v, "nx": nx, "steps": 60}
+             for k, (v, nx) in enumerate([("thermoacoustic", 30), ("thermoacoustic3", 41),
+                                          ("sync", 30), ("sync_exp", 25)])]
+
+
+def make_coupling():
+    from oracle.ref_loader import load_reference
+    ref = load_reference()
+    import pyfds.regions
+    ref.regions = pyfds.regions
+    out = {}
+    for case in CPL_CASES:
+        spec = scenarios.coupled_scenario(case["seed"], case["variant"], case["nx"],
+                                          case["steps"])
+        prefix = "c%d/" % case["seed"]
+        out[prefix + "digest"] = np.array(spec_digest(spec))
+        if spec["kind"] == "ThermoAcoustic1D":
+            pack_inputs(spec, out, prefix)
+        else:
+            for k, f in enumerate(spec["fields"]):
+                pack_inputs(f, out, prefix + "f%d/" % k)
+        obj = scenarios.build_coupled(ref, spec, ref_build.build_reference_field)
+        obj.simulate(spec["steps"])
+        for k, (st, sig) in enumerate(scenarios.coupled_results(obj, lambda f: type(f).__name__)):
+            for c in st:
+                out[prefix + "f%d/%s/state" % (k, c)] = st[c]
+                for j, x in enumerate(sig[c]):
+                    out[prefix + "f%d/%s/sig%d" % (k, c, j)] = x
+    out["cases"] = np.array(json.dumps(CPL_CASES))
+    np.savez_compressed(os.path.join(HERE, "coupling.npz"), **out)
+
+
 def make_workload(name, spec, keep_state, steps=None):
     t0 = time.time()
     out = {"digest": np.array(spec_digest(spec))}
@@ -170,6 +205,7 @@ def main():
         "random": make_random,
         "flow": make_flow,
         "nonlinear": make_nonlinear,
+        "coupling": make_coupling,
         "acoustic1d": lambda: make_workload("acoustic1d_water.npz",
                                             workloads.acoustic1d_water(), True),
         "axi_small": lambda: make_workload(

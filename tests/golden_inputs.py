@@ -39,11 +39,12 @@ def pack_inputs(spec, out, prefix="", materials=False):
 
 def apply_inputs(spec, g, prefix=""):
     keys = set(g.files)
-    mats = []
-    for k, (idx, params) in enumerate(spec["materials"]):
-        key = prefix + "in/mat/%d" % k
-        mats.append((g[key] if key in keys else idx, params))
-    spec["materials"] = mats
+    if "materials" in spec:
+        mats = []
+        for k, (idx, params) in enumerate(spec["materials"]):
+            key = prefix + "in/mat/%d" % k
+            mats.append((g[key] if key in keys else idx, params))
+        spec["materials"] = mats
     for name in list((spec.get("init") or {}).keys()):
         key = prefix + "in/init/" + name
         keyc = prefix + "in/initc/" + name

@@ -380,3 +380,27 @@ def test_nonlinear_1d_sim_step_loop_equals_simulate(gpu):
         assert np.array_equal(sa[c], sb[c])
         for x, y in zip(ga[c], gb[c]):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_coupled_fields_vs_reference(gpu, exact):
+    """ThermoAcoustic1D and SynchronizedFields: every field steps on the GPU, the
+    interactions run on the host copies. Exact mode is bit-identical except where a
+    transfer function calls np.exp on the host (its last bit may differ between the
+    machine that made the fixture and this one): there the 1e-12 bar applies."""
+    import pyfds_gb300
+    from coupled_helpers import compare, coupled_spec, kind_of
+    from oracle import scenarios as S2
+    g = golden("coupling.npz")
+    for case in json.loads(str(g["cases"])):
+        spec, prefix = coupled_spec(case, g)
+        obj = S2.build_coupled(pyfds_gb300, spec, build_field, exact=exact)
+        obj.simulate(spec["steps"])
+        bitwise = exact and case["variant"] != "sync_exp"
+
+        def check(a, b, where):
+            if bitwise:
+                assert np.array_equal(a, b), (case, where, np.max(np.abs(a - b)))
+            else:
+                assert rel_l2(a, b) <= TOL, (case, where, rel_l2(a, b))
+        compare(S2.coupled_results(obj, kind_of), g, prefix, check)

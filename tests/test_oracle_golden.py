@@ -271,3 +271,18 @@ def test_oracle_nonlinear_bitwise():
             assert np.array_equal(st[c], g[prefix + c + "/state"]), (case, c)
             for j, s in enumerate(sig[c]):
                 assert np.array_equal(s, g[prefix + c + "/sig%d" % j]), (case, c, j)
+
+
+def test_oracle_coupling_bitwise():
+    """Coupled fields (pyfds/coupling.py, pyfds/coupled_fields.py): the oracle's
+    SynchronizedFields stepping against the reference's trajectories, bit for bit."""
+    from coupled_helpers import compare, coupled_spec
+    from golden_digest import spec_digest
+    g = _load("coupling.npz")
+    for case in json.loads(str(g["cases"])):
+        spec, prefix = coupled_spec(case, g)
+        assert str(g[prefix + "digest"]) == spec_digest(spec), "scenario generator drifted"
+
+        def check(a, b, where):
+            assert np.array_equal(a, b), (case, where)
+        compare(O.simulate_coupled(spec, spec["steps"]), g, prefix, check)
