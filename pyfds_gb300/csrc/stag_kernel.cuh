@@ -99,6 +99,17 @@ __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
   return StepInfo{a.step, a.step0, a.apply_next, a.store_flux};
 }
 
+// Resident CTAs per SM the 256-thread 2-D tile kernels are compiled for (the
+// register budget per thread follows: 65536 / (256 x blocks)). Measured on the
+// 2048^2 acoustic step: float64 potential 5 (4: -2 %, 6 spills and loses 6 %),
+// float32 potential 6 (4: -8 %).
+#ifndef FDS_STAG_BLOCKS_256_F64
+#define FDS_STAG_BLOCKS_256_F64 5
+#endif
+#ifndef FDS_STAG_BLOCKS_256_F32
+#define FDS_STAG_BLOCKS_256_F32 6
+#endif
+
 // Variant switches of the tile kernel.
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
           bool EXACT_, int STAGES_ = 1>
@@ -117,7 +128,17 @@ struct StagCfg {
   static constexpr int RX = TX + 8;          // region columns x0-4 .. x0+TX+3
   static constexpr int RY = HAS_V ? TY + 3 : TY;
   static constexpr int RN = RX * RY;
+  // CTAs per SM of the batched kernel (more registers per thread than the
+  // single-field kernel: a tighter budget spills)
   static constexpr int MIN_BLOCKS = STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : 4) : 2);
+  // CTAs per SM of the single-field kernel for a potential of `psize` bytes per value
+  static constexpr int min_blocks(int psize) {
+    return STAGES == 2 ? 1
+                       : (HAS_V ? (NT >= 512 ? 2
+                                             : (psize == 4 ? FDS_STAG_BLOCKS_256_F32
+                                                           : FDS_STAG_BLOCKS_256_F64))
+                                : 2);
+  }
 };
 
 template <typename T>
@@ -617,7 +638,7 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
 // the current tile is computed from the other buffer. Staging is TMA when the
 // launch provides tensor maps (use_tma) and cp.async otherwise.
 template <class C, typename TP, typename TF, typename TC>
-__global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
+__global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP)))
     stag_step_kernel(const __grid_constant__ StagArgs<TP, TF, TC> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const bool iso = a.iso || !C::HAS_V;
