@@ -249,10 +249,14 @@ typedef struct FdsNl1dProblem {
   const double* rho0;/* [n] static density */
   const double* e1;  /* [n] state-equation factor (see above) */
   const double* e2;  /* [n] state-equation factor or exponent (see above) */
+  uint32_t* sync;    /* device uint32: the grid barrier's arrival counter (scratch; zeroed
+                        by the call; calls sharing it must be stream-ordered) */
+  int32_t* status;   /* device int32 the kernel ORs FDS_STATUS_* bits into, or NULL */
 } FdsNl1dProblem;
 
-/* Advances a nonlinear 1-D field by nsteps steps in one launch (one CTA loops over
- * the steps; the grid is small). state->cur/nxt: pressure (updated in place in cur),
+/* Advances a nonlinear 1-D field by nsteps steps in one cooperative launch: one CTA
+ * per tile of tile_x cells loops over the steps, with two grid-wide barriers per step
+ * (bounded waits; FDS_STATUS_TMA_TIMEOUT is reported if one gives up). state->cur/nxt: pressure (updated in place in cur),
  * velocity and density (ping-pong, swapped per step like fds_stag_run). tables->comp:
  * pressure, velocity, density. Replaces the loop of Field.simulate around
  * IdealGas1D.sim_step / Acoustic2ndOrder1D.sim_step (pyfds/nonlinear_acoustics.py:55-90,

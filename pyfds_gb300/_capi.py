@@ -106,7 +106,8 @@ assert PROBE_DTYPE.itemsize == 16
 class FdsNl1dProblem(C.Structure):
     _fields_ = [("kind", C.c_int32), ("flags", C.c_uint32), ("n", C.c_int32),
                 ("tile_x", C.c_int32), ("f1", C.c_double), ("fc", C.c_double),
-                ("a", C.c_void_p), ("rho0", C.c_void_p), ("e1", C.c_void_p), ("e2", C.c_void_p)]
+                ("a", C.c_void_p), ("rho0", C.c_void_p), ("e1", C.c_void_p), ("e2", C.c_void_p),
+                ("sync", C.c_void_p), ("status", C.c_void_p)]
 
 
 class FdsConvArgs(C.Structure):

@@ -1,21 +1,30 @@
 // Nonlinear 1-D acoustics (IdealGas1D, Acoustic2ndOrder1D; pyfds/nonlinear_acoustics.py).
 //
-// The grids of these fields are small (hundreds to thousands of cells) and the steps
-// many, so one CTA runs every step of a call in one launch: the phases of a step
-// (pressure bounds/outputs, velocity update, velocity bounds/outputs, density update,
-// density bounds/outputs, state equation) are separated by block barriers, and the
-// state stays in L1/L2. Each DIA product is formed in scipy's accumulation order
-// (y = 0, then one diagonal after the other); with FDS_FLAG_EXACT every operation is
-// an unfused IEEE operation, so the result is the reference's bit for bit except
-// where the ideal-gas state equation calls pow (the device pow and the host's libm
-// may differ in the last bit).
+// These grids are small (hundreds to thousands of cells) and the steps many, so every
+// step of a call runs in one cooperative launch: CTA b owns tile b (tile_x cells) and
+// loops over the steps. A step's phases (pressure bounds/outputs, velocity update and
+// bounds/outputs, density update and bounds/outputs, state equation) touch a
+// neighbour's cell in two places only: the velocity update reads p[i-1], the density
+// update reads v[i+1] and d[i+1]. So two grid-wide barriers per step suffice: after
+// the pressure bounds and after the velocity bounds. (Ping-pong buffers for v and d
+// keep every other read ahead of the next overwrite by at least one barrier.) Each
+// CTA applies the boundary groups and probes of its own tile, which the host tables
+// bucket per tile. Spreading the cells over many SMs matters on GB300: the state
+// equation's pow and the divisions run on the FP64 pipe, about 2 FMAs per clock per SM.
+//
+// Each DIA product is formed in scipy's accumulation order (y = 0, then one diagonal
+// after the other); with FDS_FLAG_EXACT every operation is an unfused IEEE operation,
+// so the result is the reference's bit for bit except where the ideal-gas state
+// equation calls pow (the device pow and the host's libm may differ in the last bit).
+#include <utility>
+
 #include "fds_capi.h"
 #include "fds_internal.h"
 
 namespace fds {
 namespace {
 
-constexpr int kNlThreads = 1024;
+constexpr long long kBarrierLimit = 1ll << 22;
 
 template <bool EXACT>
 struct Ops {
@@ -36,18 +45,21 @@ struct NlArgs {
   double f1, fc;
   FdsCompTables tab[3];
   const double* pool;
-  int n, ntiles;
+  unsigned* sync;
+  int32_t* status;
+  int n, tile, ntiles;
   int64_t step0;
   int32_t nsteps;
 };
 
-// values[idx] = additive * old + value, in list order (pyfds/regions.py:125-145)
+// values[idx] = additive * old + value, in list order (pyfds/regions.py:125-145), for
+// the boundary groups of tile `t`
 template <bool EXACT>
-__device__ void apply_bounds(const FdsCompTables& tb, int ntiles, double* x, const double* pool,
+__device__ void apply_bounds(const FdsCompTables& tb, int t, double* x, const double* pool,
                              int64_t step) {
   if (!tb.bound_tile_start) return;
-  const int e = tb.bound_tile_start[ntiles];
-  for (int g = threadIdx.x; g < e; g += blockDim.x) {
+  const int e = tb.bound_tile_start[t + 1];
+  for (int g = tb.bound_tile_start[t] + threadIdx.x; g < e; g += blockDim.x) {
     const FdsBoundGroup grp = tb.groups[g];
     double val = x[grp.cell];
     for (int o = grp.op_begin; o < grp.op_end; ++o) {
@@ -61,33 +73,62 @@ __device__ void apply_bounds(const FdsCompTables& tb, int ntiles, double* x, con
   }
 }
 
-__device__ void write_probes(const FdsCompTables& tb, int ntiles, const double* x, int64_t row) {
+__device__ void write_probes(const FdsCompTables& tb, int t, const double* x, int64_t row) {
   if (!tb.probe_tile_start || tb.out_rows <= 0) return;
-  const int e = tb.probe_tile_start[ntiles];
+  const int e = tb.probe_tile_start[t + 1];
   double* out = tb.out + row * (int64_t)tb.ncols;
-  for (int q = threadIdx.x; q < e; q += blockDim.x) {
+  for (int q = tb.probe_tile_start[t] + threadIdx.x; q < e; q += blockDim.x) {
     const FdsProbe pr = tb.probes[q];
     out[pr.col] = x[pr.cell];
   }
 }
 
+// Grid-wide barrier number k (0-based) of this launch: every CTA adds one to the
+// counter and waits until it reaches (k + 1) * gridDim.x. Bounded: false if the wait
+// gave up.
+__device__ bool grid_barrier(unsigned* count, unsigned k) {
+  __syncthreads();
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    const unsigned target = (k + 1) * gridDim.x;
+    long long i = 0;
+    const volatile unsigned* c = count;
+    while (*c < target) {
+      if (++i > kBarrierLimit) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(16);
+    }
+    __threadfence();
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
 template <bool EXACT, int KIND, bool CONV, bool NLS>
-__global__ void __launch_bounds__(kNlThreads) nl1d_kernel(const NlArgs a) {
+__global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
   using O = Ops<EXACT>;
   const int n = a.n;
+  const int t = blockIdx.x;
+  const int c0 = t * a.tile;
+  const int c1 = min(n, c0 + a.tile);
   const double f1 = a.f1, fc = a.fc;
   double* p = a.p;
+  unsigned k = 0;
   for (int32_t s = 0; s < a.nsteps; ++s) {
     const int64_t step = a.step0 + s;
     const double* v = a.v[s & 1];
     double* vn = a.v[(s & 1) ^ 1];
     const double* r = a.r[s & 1];
     double* rn = a.r[(s & 1) ^ 1];
-    apply_bounds<EXACT>(a.tab[0], a.ntiles, p, a.pool, step);
+    apply_bounds<EXACT>(a.tab[0], t, p, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[0], a.ntiles, p, s);
+    write_probes(a.tab[0], t, p, s);
+    if (!grid_barrier(a.sync, k++)) break;
     // velocity: v - ((a_v_p p) / B [+ a_v_v2 v] - (a_v_v v) / B), B = rho0 + d
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       double t1 = 0.0;  // backward difference: diagonals -1 (-f1) then 0 (f1)
       if (i >= 1) t1 = O::add(t1, O::mul(-f1, p[i - 1]));
       t1 = O::add(t1, O::mul(f1, p[i]));
@@ -107,22 +148,24 @@ __global__ void __launch_bounds__(kNlThreads) nl1d_kernel(const NlArgs a) {
       vn[i] = O::sub(v[i], term);
     }
     __syncthreads();
-    apply_bounds<EXACT>(a.tab[1], a.ntiles, vn, a.pool, step);
+    apply_bounds<EXACT>(a.tab[1], t, vn, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[1], a.ntiles, vn, s);
+    write_probes(a.tab[1], t, vn, s);
+    if (!grid_barrier(a.sync, k++)) break;
     // density: d - a_d_v ((d + rho0) v), forward difference: diagonals 0 (-f1), +1 (f1)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       const double w0 = O::mul(O::add(r[i], a.rho0[i]), vn[i]);
-      double t = O::add(0.0, O::mul(-f1, w0));
-      if (i + 1 < n) t = O::add(t, O::mul(f1, O::mul(O::add(r[i + 1], a.rho0[i + 1]), vn[i + 1])));
-      rn[i] = O::sub(r[i], t);
+      double tt = O::add(0.0, O::mul(-f1, w0));
+      if (i + 1 < n)
+        tt = O::add(tt, O::mul(f1, O::mul(O::add(r[i + 1], a.rho0[i + 1]), vn[i + 1])));
+      rn[i] = O::sub(r[i], tt);
     }
     __syncthreads();
-    apply_bounds<EXACT>(a.tab[2], a.ntiles, rn, a.pool, step);
+    apply_bounds<EXACT>(a.tab[2], t, rn, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[2], a.ntiles, rn, s);
-    // state equation
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    write_probes(a.tab[2], t, rn, s);
+    // state equation (own cells)
+    for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       const double d = rn[i];
       double pv;
       if (KIND == FDS_NL1D_IDEAL_GAS) {
@@ -139,18 +182,21 @@ __global__ void __launch_bounds__(kNlThreads) nl1d_kernel(const NlArgs a) {
     }
     __syncthreads();
   }
+  if (k < 2u * (unsigned)a.nsteps && threadIdx.x == 0 && a.status)
+    atomicOr(a.status, FDS_STATUS_TMA_TIMEOUT);
 }
 
+using NlKernel = void (*)(NlArgs);
+
 template <bool EXACT>
-void launch(const NlArgs& a, int kind, bool conv, bool nls, cudaStream_t s) {
+NlKernel pick(int kind, bool conv, bool nls) {
   if (kind == FDS_NL1D_IDEAL_GAS) {
-    if (conv && nls) nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, true><<<1, kNlThreads, 0, s>>>(a);
-    else if (conv) nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, false><<<1, kNlThreads, 0, s>>>(a);
-    else if (nls) nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, true><<<1, kNlThreads, 0, s>>>(a);
-    else nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, false><<<1, kNlThreads, 0, s>>>(a);
-  } else {
-    nl1d_kernel<EXACT, FDS_NL1D_SECOND_ORDER, true, false><<<1, kNlThreads, 0, s>>>(a);
+    if (conv && nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, true>;
+    if (conv) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, false>;
+    if (nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, true>;
+    return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, false>;
   }
+  return nl1d_kernel<EXACT, FDS_NL1D_SECOND_ORDER, true, false>;
 }
 
 }  // namespace
@@ -165,8 +211,8 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
     return set_error(FDS_E_ARG, "bad grid, tiling or step range");
   if (prob->kind != FDS_NL1D_IDEAL_GAS && prob->kind != FDS_NL1D_SECOND_ORDER)
     return set_error(FDS_E_ARG, "unknown nonlinear kind %d", prob->kind);
-  if (!prob->a || !prob->rho0 || !prob->e1 || !prob->e2)
-    return set_error(FDS_E_ARG, "missing coefficient arrays");
+  if (!prob->a || !prob->rho0 || !prob->e1 || !prob->e2 || !prob->sync)
+    return set_error(FDS_E_ARG, "missing coefficient arrays or barrier counter");
   for (int k = 0; k < 3; ++k) {
     if (!st->cur[k] || (k > 0 && !st->nxt[k])) return set_error(FDS_E_ARG, "missing state buffer %d", k);
     const FdsCompTables& t = tables->comp[k];
@@ -174,6 +220,9 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
       return set_error(FDS_E_ARG, "output buffer of component %d too small", k);
   }
   if (nsteps == 0) return FDS_OK;
+  const int ntiles = (prob->n + prob->tile_x - 1) / prob->tile_x;
+  if ((int64_t)2 * nsteps * ntiles >= 0xffffffffll)
+    return set_error(FDS_E_SIZE, "too many steps x tiles for one call");
   NlArgs a{};
   a.p = (double*)st->cur[0];
   a.v[0] = (double*)st->cur[1];
@@ -188,18 +237,32 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
   a.fc = prob->fc;
   for (int k = 0; k < 3; ++k) a.tab[k] = tables->comp[k];
   a.pool = tables->pool;
+  a.sync = prob->sync;
+  a.status = prob->status;
   a.n = prob->n;
-  a.ntiles = (prob->n + prob->tile_x - 1) / prob->tile_x;
+  a.tile = prob->tile_x;
+  a.ntiles = ntiles;
   a.step0 = step0;
   a.nsteps = nsteps;
   const bool conv = prob->kind == FDS_NL1D_SECOND_ORDER || (prob->flags & FDS_NL1D_CONVECTIVE);
   const bool nls = (prob->flags & FDS_NL1D_NL_STATE) != 0;
+  NlKernel fn = (prob->flags & FDS_FLAG_EXACT) ? pick<true>(prob->kind, conv, nls)
+                                               : pick<false>(prob->kind, conv, nls);
+  const int threads = prob->tile_x < 256 ? ((prob->tile_x + 31) / 32) * 32 : 256;
+  // every CTA waits for the others at the grid barriers: all must be resident
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, threads, 0);
+  if (!coop || (int64_t)per_sm * sms < ntiles)
+    return set_error(FDS_E_SIZE, "%d tiles cannot all be resident (%d per SM x %d SMs)", ntiles,
+                     per_sm, sms);
   cudaStream_t s = (cudaStream_t)stream;
-  if (prob->flags & FDS_FLAG_EXACT)
-    launch<true>(a, prob->kind, conv, nls, s);
-  else
-    launch<false>(a, prob->kind, conv, nls, s);
-  const cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaMemsetAsync(prob->sync, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "barrier reset: %s", cudaGetErrorString(e));
+  void* params[] = {&a};
+  e = cudaLaunchCooperativeKernel((const void*)fn, dim3(ntiles), dim3(threads), params, 0, s);
   if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "nonlinear 1-D launch: %s", cudaGetErrorString(e));
   // velocity and density were ping-ponged once per step
   if (nsteps & 1)

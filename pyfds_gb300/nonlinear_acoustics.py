@@ -5,7 +5,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _capi
+from . import _capi, _tables
 from . import acoustics as ac
 from . import fields as fld
 from ._engine import StagEngine, require_cuda
@@ -17,7 +17,18 @@ __all__ = [
 
 
 class _NlEngine(StagEngine):
-    """StagEngine whose launch is the nonlinear 1-D step (same buffers and tables)."""
+    """StagEngine whose launch is the nonlinear 1-D step (same buffers and tables,
+    bucketed per tile of ``tile_cells`` cells: one CTA per tile)."""
+
+    @staticmethod
+    def tile_cells(n):
+        """64 cells per CTA (spreads the FP64 work over SMs), more for fields above
+        512 tiles so that every CTA stays resident."""
+        return 64 * max(1, -(-n // (64 * 512)))
+
+    def _geometry(self):
+        n = self.field.num_points
+        return _tables.TileGeometry(n, 1, self.tile_cells(n), 1, False, 0)
 
     def launch(self, plan):
         torch = require_cuda()
@@ -31,6 +42,10 @@ class _NlEngine(StagEngine):
         prob.fc = f._nl_scalars["fc"]
         for name in ("a", "rho0", "e1", "e2"):
             setattr(prob, name, self.coef_tensors[name].data_ptr())
+        if getattr(self, "_sync", None) is None:
+            self._sync = torch.zeros(1, dtype=torch.int32, device=self.coef_tensors["a"].device)
+        prob.sync = self._sync.data_ptr()
+        prob.status = self.status.data_ptr() if self.status is not None else None
         names = f._stag_components
         state = _capi.FdsStagState()
         for k in range(3):
