@@ -536,6 +536,32 @@ def run_surrogate(args):
     return 0
 
 
+def run_coupling_study(args):
+    """ThermoAcoustic1D (1000 cells, coupling every 3 steps, accumulated): the
+    one-call library stepping against the reference's loop (fields stepped one by
+    one, coupling on the host copies), same field, same steps."""
+    import torch
+    import pyfds_gb300
+    from oracle import scenarios
+    from pyfds_gb300 import workloads
+    out = {"study": "ThermoAcoustic1D 1000 cells, stepping 3 (accumulated), 500 steps"}
+    for native in (True, False):
+        spec = scenarios.coupled_scenario(5, "thermoacoustic3", nx=1000, steps=2000)
+        obj = scenarios.build_coupled(pyfds_gb300, spec, workloads.build_field)
+        if not native:
+            obj._native_path = lambda: False
+        obj.simulate(10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        obj.simulate(500)
+        torch.cuda.synchronize()
+        us = (time.perf_counter() - t0) / 500 * 1e6
+        out["native_us_per_step" if native else "step_by_step_us_per_step"] = us
+    out["speedup"] = out["step_by_step_us_per_step"] / out["native_us_per_step"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_surrogate_iter(args):
     """A few surrogate training iterations (batch 32 at 256^2, a 32-pair solver
     dataset) after 3 warm-up iterations: the small case the kernel profiles use."""
@@ -717,7 +743,7 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")
     ap.add_argument("--study", default="",
                     choices=["", "precision", "axi", "thermal", "batched", "surrogate",
-                             "surrogate-iter"],
+                             "surrogate-iter", "coupling"],
                     help="print the precision study (float32 paths against float64) or the "
                          "learned-surrogate study instead")
     ap.add_argument("--surr-instances", type=int, default=625,
@@ -739,6 +765,8 @@ def main():
         return run_surrogate(args)
     if args.study == "surrogate-iter":
         return run_surrogate_iter(args)
+    if args.study == "coupling":
+        return run_coupling_study(args)
     if args.study:
         return run_study(args)
     if args.workload == "batched":

@@ -264,6 +264,24 @@ typedef struct FdsNl1dProblem {
 int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps, void* stream);
 
+/* ThermoAcoustic1D (pyfds/coupled_fields.py:10-65) for nsteps steps in one call: per
+ * step the acoustic step, the thermal step (both as fds_stag_run for one step; output
+ * row = step - step0) and the loss coupling of BoundaryCoupling.apply
+ * (pyfds/coupling.py:121-140) from the acoustic velocity into the temperature:
+ *   loss = g * (a_v_p (v * rho_ac))^2 * dt, with a_v_p the acoustic backward
+ *   difference of factor bx = dt/dx/rho_ac and g = (mu / rho_th) / c_th;
+ *   stepping == 1 and !accumulate: T += loss every step; accumulate: acc += loss every
+ *   step and, when step % stepping == 0, T += acc and acc is emptied; otherwise
+ *   T += loss when step % stepping == 0.
+ * acc: [n] device accumulator; *acc_empty (host, in/out) says it holds nothing yet.
+ * Both problems must be float64 1-D fields of the same size. */
+int32_t fds_thermoacoustic_run(const FdsStagProblem* acoustic, FdsStagState* ac_state,
+                               const FdsStagTables* ac_tables, const FdsStagProblem* thermal,
+                               FdsStagState* th_state, const FdsStagTables* th_tables,
+                               const double* g, const double* rho_ac, double* acc,
+                               int32_t* acc_empty, double dt, int32_t stepping,
+                               int32_t accumulate, int64_t step0, int32_t nsteps, void* stream);
+
 /* The moving-medium shift of one step alone, in place on state->cur (p, vx, vy):
  * replaces AcousticFlow2D.apply_flow (pyfds/acoustic_flow.py:49-57) for callers that
  * step a flow field themselves. Needs FDS_FLAG_FLOW and flow_period. */

@@ -404,3 +404,29 @@ def test_coupled_fields_vs_reference(gpu, exact):
             else:
                 assert rel_l2(a, b) <= TOL, (case, where, rel_l2(a, b))
         compare(S2.coupled_results(obj, kind_of), g, prefix, check)
+
+
+@pytest.mark.parametrize("variant", ["thermoacoustic", "thermoacoustic3"])
+def test_thermoacoustic_native_equals_step_by_step(gpu, variant, monkeypatch):
+    """ThermoAcoustic1D's one-call stepping (fds_thermoacoustic_run) against the
+    reference's loop (fields stepped one by one, coupling applied on the host), both
+    exact; simulate is split into two chunks so that an accumulated transfer crosses
+    a call boundary."""
+    import pyfds_gb300
+    from coupled_helpers import kind_of
+    from oracle import scenarios as S2
+    spec = S2.coupled_scenario(77, variant, nx=45, steps=27)
+    a = S2.build_coupled(pyfds_gb300, spec, build_field, exact=True)
+    assert a._native_path()
+    a.simulate(7)
+    a.simulate(20)
+    b = S2.build_coupled(pyfds_gb300, spec, build_field, exact=True)
+    monkeypatch.setattr(type(b), "_native_path", lambda self: False)
+    b.simulate(7)
+    b.simulate(20)
+    assert a.step == b.step == 27
+    for (sa, ga), (sb, gb) in zip(S2.coupled_results(a, kind_of), S2.coupled_results(b, kind_of)):
+        for c in sa:
+            assert np.array_equal(sa[c], sb[c]), c
+            for x, y in zip(ga[c], gb[c]):
+                assert np.array_equal(x, y), c
