@@ -56,6 +56,33 @@ def _dist():
     return ws, rank, local
 
 
+def _init_replicas(backend="nccl"):
+    """Join the process group of a multi-replica run (WORLD_SIZE > 1): one
+    independent replica per rank, no data-path collective. Returns (ws, rank, local)."""
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def _max_over_ranks(ms, device="cuda"):
+    """The slowest replica's time: the job's time for weak-scaled replicas."""
+    ws, _, _ = _dist()
+    if ws == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -187,11 +214,7 @@ def run_batched(args):
     """The layered-media batch: one launch per step for all instances, the whole
     run replayed from a CUDA graph; e2e through simulate_batch with host buffers."""
     import torch
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ws, rank, local = _init_replicas()
     from pyfds_gb300 import workloads
     from pyfds_gb300.batch import BatchRunner, simulate_batch
     builder, kwargs, balg = WORKLOADS["batched"]
@@ -241,12 +264,7 @@ def run_batched(args):
             e1.synchronize()
             total_ms += e0.elapsed_time(e1)
     barrier()
-    ms = total_ms / args.steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = _max_over_ranks(total_ms / args.steps)
     value = ws * cells * nt / (ms * 1e-3) / 1e9
     launch_ms = ms / nt
     # e2e: the public API with host state and host outputs, every step
@@ -579,11 +597,7 @@ def run_surrogate_iter(args):
 
 def run_ours(args):
     import torch
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ws, rank, local = _init_replicas()
     dev = torch.device("cuda", torch.cuda.current_device())
     from pyfds_gb300 import workloads, _capi
     builder, kwargs, balg = WORKLOADS[args.workload]
@@ -628,12 +642,7 @@ def run_ours(args):
             eng.launch(plan)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = _max_over_ranks(ev0.elapsed_time(ev1) / args.steps, device=dev)
     value = ws * cells * nt / (ms * 1e-3) / 1e9
     # step kernel alone: average launch over a timed run without the state reset
     ev2 = torch.cuda.Event(enable_timing=True)

@@ -430,3 +430,47 @@ def test_thermoacoustic_native_equals_step_by_step(gpu, variant, monkeypatch):
             assert np.array_equal(sa[c], sb[c]), c
             for x, y in zip(ga[c], gb[c]):
                 assert np.array_equal(x, y), c
+
+
+@pytest.mark.parametrize("kind,nx,ny", [("Acoustic2D", 1, 1), ("Acoustic2D", 1, 7),
+                                        ("Acoustic2D", 7, 1), ("Acoustic2D", 2, 2),
+                                        ("Thermal2D", 1, 5), ("Acoustic1D", 1, None),
+                                        ("Thermal1D", 3, None)])
+def test_degenerate_grids_vs_oracle(gpu, kind, nx, ny):
+    """Grids of one row, one column, one cell: exact mode against the oracle."""
+    spec = S.random_scenario(900 + nx * 10 + (ny or 0), kind, nx, ny, steps=9)
+    f = build_field(spec, exact=True)
+    f.simulate(spec["steps"])
+    st, sig = field_results(f)
+    ref_st, ref_sig = O.simulate(spec, spec["steps"])
+    for c in st:
+        assert np.array_equal(st[c], ref_st[c]), c
+        for x, y in zip(sig[c], ref_sig[c]):
+            assert np.array_equal(x, y), c
+
+
+def test_largest_grid_scales_exactly(gpu):
+    """8192^2 cells (the largest grid in the tests; 4.3 GB of state and coefficients):
+    exact-mode time stepping is linear in the state and the sources, and scaling both
+    by 2 is exact in IEEE arithmetic, so every value and output must double bit for
+    bit."""
+    n, steps = 8192, 6
+    spec = workloads.acoustic2d_steel_block(n=n, nt=steps, n_probes=16)
+    rng = np.random.default_rng(5)
+    p0 = rng.standard_normal(n * n) * 1e-3
+    results = []
+    for k in (1.0, 2.0):
+        sp = dict(spec)
+        sp["init"] = {"pressure": k * p0}
+        sp["bounds"] = {"pressure": [dict(b, value=k * np.asarray(b["value"]))
+                                     for b in spec["bounds"]["pressure"]]}
+        f = build_field(sp, exact=True)
+        f.simulate(steps)
+        results.append(field_results(f))
+        del f
+    (s1, g1), (s2, g2) = results
+    for c in s1:
+        assert np.array_equal(2.0 * s1[c], s2[c]), c
+        assert np.count_nonzero(s1[c]) > 0
+        for x, y in zip(g1[c], g2[c]):
+            assert np.array_equal(2.0 * x, y), c
