@@ -166,8 +166,7 @@ def load(path=None):
     path = path or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(
-            "libfdsgpu.so is not built (%s); run `python -c \"import __graft_entry__ as g; "
-            "g.build()\"` or `python -m pyfds_gb300._build`" % path)
+            "libfdsgpu.so is not built (%s); run `python -m pyfds_gb300._build`" % path)
     lib = C.CDLL(path)
     lib.fds_abi_version.restype = C.c_int32
     lib.fds_abi_version.argtypes = []

@@ -410,9 +410,11 @@ _ZEROS = {}
 
 
 def _zeros_i32(torch, n, dev):
-    if n not in _ZEROS:
-        _ZEROS[n] = torch.zeros(n, dtype=torch.int32, device=dev)
-    return _ZEROS[n]
+    """A cached device vector of n int32 zeros (the snapshot index of every sample)."""
+    key = (str(dev), n)
+    if key not in _ZEROS:
+        _ZEROS[key] = torch.zeros(n, dtype=torch.int32, device=dev)
+    return _ZEROS[key]
 
 
 def rel_l2(net, a, b, zref, inst):

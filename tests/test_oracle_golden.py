@@ -170,7 +170,7 @@ def test_oracle_acoustic1d_water_bitwise():
     assert np.array_equal(sig["pressure"][0], g["pressure/sig0"])
     assert np.array_equal(st["pressure"], g["pressure/state"])
     assert np.array_equal(st["velocity"], g["velocity/state"])
-    # the source pulse reaches the probe with the amplitude the survey recorded
+    # the source pulse reaches the probe at index 800 with a peak |p| of 0.807
     assert abs(np.abs(sig["pressure"][0]).max() - 0.807) < 0.01
 
 
