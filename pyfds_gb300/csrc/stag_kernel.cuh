@@ -109,6 +109,9 @@ __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
 #ifndef FDS_STAG_BLOCKS_256_F32
 #define FDS_STAG_BLOCKS_256_F32 6
 #endif
+#ifndef FDS_BATCH_BLOCKS_256
+#define FDS_BATCH_BLOCKS_256 4
+#endif
 
 // Variant switches of the tile kernel.
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
@@ -130,7 +133,8 @@ struct StagCfg {
   static constexpr int RN = RX * RY;
   // CTAs per SM of the batched kernel (more registers per thread than the
   // single-field kernel: a tighter budget spills)
-  static constexpr int MIN_BLOCKS = STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : 4) : 2);
+  static constexpr int MIN_BLOCKS =
+      STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : FDS_BATCH_BLOCKS_256) : 2);
   // CTAs per SM of the single-field kernel for a potential of `psize` bytes per value
   static constexpr int min_blocks(int psize) {
     return STAGES == 2 ? 1
