@@ -83,6 +83,14 @@ def _max_over_ranks(ms, device="cuda"):
     return float(t.item())
 
 
+def _max_sm_mhz():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return float(json.load(fh).get("sm_max_mhz", 2070.0))
+    return 2070.0
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -92,12 +100,13 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_from_profiles(key):
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summaries."""
+def _traffic_from_profiles(key, what="traffic_bytes_per_launch"):
+    """A per-launch figure of the step kernel (DRAM bytes, or DFMA instructions with
+    ``what="dfma_per_launch"``) from the committed ncu summaries."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None
-    pat = re.compile(r"traffic_bytes_per_launch\[%s\]\s*[:=]\s*([0-9.eE+]+)" % re.escape(key))
+    pat = re.compile(r"%s\[%s\]\s*[:=]\s*([0-9.eE+]+)" % (re.escape(what), re.escape(key)))
     for name in sorted(os.listdir(pdir)):
         if not name.endswith((".md", ".txt")):
             continue
@@ -720,6 +729,18 @@ def run_ours(args):
             # moving medium, the row shift and the next step's pressure bounds)
             "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else
                                               1 if args.workload == "nonlinear1d" else nt + 1))}
+    dfma = _traffic_from_profiles("%s_%s" % (args.workload, args.precision), "dfma_per_launch")
+    if dfma and launch_ms:
+        # the FP64 pipe bounds the float64 step: its roofline beside the HBM one. Peak =
+        # 2 DFMA per clock per SM (ncu's peak_sustained of the DFMA counter) x SMs x the
+        # maximum SM clock
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_g = 2.0 * sms * _max_sm_mhz() * 1e6 / 1e9
+        got_g = dfma / (launch_ms * 1e-3) / 1e9
+        line["fp64_pipe"] = {"dfma_per_launch": dfma, "achieved_gdfma_s": got_g,
+                             "peak_gdfma_s": peak_g, "frac": got_g / peak_g,
+                             "peak_kind": "2 per clock per SM x %d SMs x %.0f MHz"
+                                          % (sms, _max_sm_mhz())}
     if args.time_steps:
         line["config"]["note"] = "time axis shortened for profiling; not a benchmark value"
     if ws == 1 and not args.no_cpu_baseline:
