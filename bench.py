@@ -2,7 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload acoustic2d|acoustic1d|axi|thermal|batched|flow|nonlinear1d]
-                    [--precision f64|f32|f32_t64]
+                    [--precision f64|f32|f32_t64|dw]
 
 One benchmark step is one full ``simulate()`` of the workload (default: the
 2048 x 2048 water/steel Acoustic2D field, 4000 time steps, float64). Prints one
@@ -32,14 +32,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (workload builder, kwargs, bytes per cell-update at f64 / f32 / f32_t64)
-    "acoustic2d": ("acoustic2d_steel_block", {}, {"f64": 64, "f32": 32}),
-    "acoustic1d": ("acoustic1d_water", {}, {"f64": 48, "f32": 24}),
-    "axi": ("axi_disc_source", {}, {"f64": 64, "f32": 32}),
-    "thermal": ("thermal2d_two_materials", {"nt": 2000}, {"f64": 32, "f32": 16, "f32_t64": 24}),
-    "batched": ("layered_media_batch", {}, {"f64": 64, "f32": 32}),
+    # name: (workload builder, kwargs, bytes per cell-update at f64 / f32 / f32_t64;
+    # double words (dw) move the float64 bytes)
+    "acoustic2d": ("acoustic2d_steel_block", {}, {"f64": 64, "f32": 32, "dw": 64}),
+    "acoustic1d": ("acoustic1d_water", {}, {"f64": 48, "f32": 24, "dw": 48}),
+    "axi": ("axi_disc_source", {}, {"f64": 64, "f32": 32, "dw": 64}),
+    "thermal": ("thermal2d_two_materials", {"nt": 2000}, {"f64": 32, "f32": 16, "f32_t64": 24, "dw": 32}),
+    "batched": ("layered_media_batch", {}, {"f64": 64, "f32": 32, "dw": 64}),
     # the moving-medium shift adds 6 x 8 B per cell every `period` (10) steps
-    "flow": ("acoustic_flow_block", {}, {"f64": 64, "f32": 32}),
+    "flow": ("acoustic_flow_block", {}, {"f64": 64, "f32": 32, "dw": 64}),
     # p, v, rho read + written, 4 coefficient arrays (the whole field stays in L1/L2)
     "nonlinear1d": ("ideal_gas_column", {}, {"f64": 80}),
 }
@@ -609,6 +610,7 @@ def run_ours(args):
     ws, rank, local = _init_replicas()
     dev = torch.device("cuda", torch.cuda.current_device())
     from pyfds_gb300 import workloads, _capi
+    from pyfds_gb300._engine import split_dw
     builder, kwargs, balg = WORKLOADS[args.workload]
     kwargs = dict(kwargs)
     if args.time_steps:
@@ -633,7 +635,10 @@ def run_ours(args):
             for t in eng.buffers[name]:
                 t.zero_()
             if name in (spec.get("init") or {}):
-                eng.buffers[name][0].copy_(torch.as_tensor(spec["init"][name], device=dev,
+                v = np.asarray(spec["init"][name], dtype=np.float64).reshape(-1)
+                if args.precision == "dw":
+                    v = split_dw(v)
+                eng.buffers[name][0].copy_(torch.as_tensor(v, device=dev,
                                                            dtype=eng.buffers[name][0].dtype))
 
     plan = eng.prepare(0, nt)
@@ -704,7 +709,8 @@ def run_ours(args):
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"f64": "f64", "f32": "f32", "f32_t64": "f32+f64"}[args.precision],
+            "dtype": {"f64": "f64", "f32": "f32", "f32_t64": "f32+f64",
+                      "dw": "f32x2 (double-word)"}[args.precision],
             "data": "synthetic (seeded workload generator, no dataset)",
             "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
@@ -763,7 +769,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="acoustic2d")
-    ap.add_argument("--precision", choices=["f64", "f32", "f32_t64"], default="f64")
+    ap.add_argument("--precision", choices=["f64", "f32", "f32_t64", "dw"], default="f64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")

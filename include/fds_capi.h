@@ -50,6 +50,11 @@ extern "C" {
 #define FDS_PREC_F64 0     /* all state and coefficients float64 (the drop-in) */
 #define FDS_PREC_F32 1     /* all state and coefficients float32 */
 #define FDS_PREC_F32_T64 2 /* float32 coefficients and fluxes, float64 potential (P/T) */
+#define FDS_PREC_DW 3      /* double-word: every state and coefficient value is a pair of
+                              float32 {hi, lo} (8 bytes, value hi + lo, |lo| <= ulp(hi)/2)
+                              computed with compensated float32 arithmetic (48-bit
+                              significands); no register-marching tiles, not batched,
+                              not exact */
 
 /* FdsStagProblem.flags */
 #define FDS_FLAG_HAS_V 1u   /* second flux component (2-D fields) */
@@ -195,8 +200,9 @@ int32_t fds_abi_version(void);
  * truncated to len). Returns the message length. */
 int32_t fds_last_error(char* buf, size_t len);
 
-/* Tile shape (cells in x, y) the kernel for this problem variant uses; host-side
- * tables must be bucketed for it. Returns FDS_OK or FDS_E_NOKERNEL. */
+/* Tile shape (cells in x, y) the kernel for this problem variant uses by default;
+ * host-side tables must be bucketed for it: 1024 x 1 (1-D), 64 x 16 (2-D), 64 x 12
+ * (2-D lossless double words). Returns FDS_OK or FDS_E_NOKERNEL. */
 int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, int32_t nx,
                             int32_t ny, int32_t* tile_x, int32_t* tile_y);
 

@@ -27,6 +27,7 @@ FAMILY_THERMAL = 1
 PREC_F64 = 0
 PREC_F32 = 1
 PREC_F32_T64 = 2
+PREC_DW = 3
 
 FLAG_HAS_V = 1
 FLAG_ABSORB = 2

@@ -14,9 +14,25 @@ import numpy as np
 from . import _capi
 from . import _tables
 
-PRECISIONS = {"f64": _capi.PREC_F64, "f32": _capi.PREC_F32, "f32_t64": _capi.PREC_F32_T64}
+PRECISIONS = {"f64": _capi.PREC_F64, "f32": _capi.PREC_F32, "f32_t64": _capi.PREC_F32_T64,
+              "dw": _capi.PREC_DW}
 
 _ALIGN = 256
+
+
+def split_dw(vals):
+    """float64 values -> (n, 2) float32 double words: hi = fl32(x), lo = fl32(x - hi)
+    (x - hi is exact in float64), so hi + lo holds 48 bits of x."""
+    v = np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)
+    hi = v.astype(np.float32)
+    lo = (v - hi.astype(np.float64)).astype(np.float32)
+    return np.stack([hi, lo], axis=1)
+
+
+def join_dw(pairs):
+    """(n, 2) float32 double words -> float64 values hi + lo."""
+    pairs = np.asarray(pairs, dtype=np.float32).reshape(-1, 2)
+    return pairs[:, 0].astype(np.float64) + pairs[:, 1].astype(np.float64)
 
 
 def _torch():
@@ -77,7 +93,7 @@ class StagEngine:
         prec = self.field.precision
         if prec == "f64":
             return torch.float64, torch.float64, torch.float64
-        if prec == "f32":
+        if prec in ("f32", "dw"):  # dw: (n, 2) float32 pairs
             return torch.float32, torch.float32, torch.float32
         return torch.float64, torch.float32, torch.float32  # f32_t64: potential in float64
 
@@ -90,6 +106,9 @@ class StagEngine:
         self.coef_tensors = {}
         for name, arr in self.field._stag_coefs.items():
             if arr is None:
+                continue
+            if self.field.precision == "dw":
+                self.coef_tensors[name] = torch.from_numpy(split_dw(arr)).to(dev)
                 continue
             self.coef_tensors[name] = torch.from_numpy(
                 np.ascontiguousarray(arr, dtype=np.float64)).to(dev).to(tc)
@@ -121,17 +140,24 @@ class StagEngine:
 
     # ------------------------------------------------------------------- state
     def _potential_offset(self):
-        """Offset of the stored potential: float32 thermal fields keep T - T_ref, with
-        T_ref the field's ``potential_offset`` or the mean initial temperature (the
-        float32 spacing near 0 K of deviation is fine, near 300 K it is 2^-15 K)."""
+        """Offset of the stored potential (0 unless below). Float32 thermal fields keep
+        T - T_ref, with T_ref the field's ``potential_offset`` or the mean initial
+        temperature (the float32 spacing near 0 K of deviation is fine, near 300 K it
+        is 2^-15 K). Double-word thermal fields use ``potential_offset`` when it is
+        set: it pays when every temperature stays close to it (the 48 bits then
+        resolve the deviation), and costs accuracy on cells far from it, so there is
+        no automatic choice. The other precisions store the temperature itself."""
         if self.offset is None:
             f = self.field
-            off = getattr(f, "potential_offset", None)
-            if off is None:
-                off = 0.0
-                if f.precision == "f32" and f._stag_family == _capi.FAMILY_THERMAL:
-                    vals = np.asarray(getattr(f, f._stag_components[0])._values, dtype=np.float64)
-                    off = float(np.mean(vals)) if vals.size else 0.0
+            off = 0.0
+            if f._stag_family == _capi.FAMILY_THERMAL and f.precision in ("f32", "dw"):
+                off = getattr(f, "potential_offset", None)
+                if off is None:
+                    off = 0.0
+                    if f.precision == "f32":
+                        vals = np.asarray(getattr(f, f._stag_components[0])._values,
+                                          dtype=np.float64)
+                        off = float(np.mean(vals)) if vals.size else 0.0
             self.offset = float(off)
         return self.offset
 
@@ -140,14 +166,16 @@ class StagEngine:
         names = self.field._stag_components
         off = self._potential_offset()
         memory = self.field._stag_family == _capi.FAMILY_ACOUSTIC
+        dword = self.field.precision == "dw"
         for k, name in enumerate(names):
             comp = getattr(self.field, name)
             dt = tp if k == 0 else tf
             bufs = self.buffers.get(name)
             n = self.field.num_points
             if bufs is None:
-                cur = torch.empty(n, dtype=dt, device=dev)
-                nxt = torch.empty(n, dtype=dt, device=dev) if (k == 0 or memory) else cur
+                shape = (n, 2) if dword else (n,)
+                cur = torch.empty(shape, dtype=dt, device=dev)
+                nxt = torch.empty(shape, dtype=dt, device=dev) if (k == 0 or memory) else cur
                 bufs = self.buffers[name] = [cur, nxt]
                 comp._attach(self, name)
                 comp._where = "host"
@@ -158,12 +186,30 @@ class StagEngine:
                                      % (name, vals.size, n))
                 if k == 0 and off:
                     vals = vals - off
-                bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
+                if dword:
+                    bufs[0].copy_(torch.from_numpy(split_dw(vals)).to(dev))
+                else:
+                    bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
                 comp._where = "both"
+
+    def device_values(self, name):
+        """Current values of a component as a float64 device tensor (offset added)."""
+        torch = _torch()
+        b = self.buffers[name][0]
+        if self.field.precision == "dw":
+            v = b[:, 0].to(torch.float64) + b[:, 1].to(torch.float64)
+        else:
+            v = b.to(dtype=torch.float64)
+        if name == self.field._stag_components[0] and self.offset:
+            v = v + self.offset
+        return v
 
     def download(self, name):
         bufs = self.buffers[name]
-        v = bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
+        if self.field.precision == "dw":
+            v = join_dw(bufs[0].detach().to("cpu").numpy())
+        else:
+            v = bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
         if name == self.field._stag_components[0] and self.offset:
             v += self.offset
         return v

@@ -14,9 +14,13 @@ class StagField:
     ``FdsCoefs`` in include/fds_capi.h and the FDS_FLAG_* bits of the variant.
 
     Keyword arguments accepted by every constructor on top of the reference's:
-      precision: "f64" (default, the drop-in), "f32", or "f32_t64" (thermal:
-                 float32 fluxes with a float64 temperature). Thermal "f32" stores the
-                 temperature as a float32 deviation from ``potential_offset``.
+      precision: "f64" (default, the drop-in), "f32", "f32_t64" (thermal:
+                 float32 fluxes with a float64 temperature) or "dw" (double-word:
+                 every value a float32 pair hi + lo with 48-bit significands,
+                 compensated float32 arithmetic; float64-class accuracy on the FP32
+                 pipe; not batched). Thermal "f32" stores the temperature as a
+                 deviation from ``potential_offset`` (default: the mean initial
+                 temperature); thermal "dw" does so when ``potential_offset`` is set.
       exact:     float64 only; evaluate in the reference's operation order without
                  fused multiply-adds (bit-identical to scipy on x86-64).
       tile:      (x, y) cells per CTA for lossless 2-D fields, one of
@@ -38,7 +42,7 @@ class StagField:
         self.tile = tuple(tile) if tile is not None else None
         self.stages = 0  # 0: automatic; 1 or 2 staging buffers (see FdsStagProblem)
         # float32 thermal fields store T - potential_offset (None: the mean initial
-        # temperature at the first launch)
+        # temperature at the first launch); double-word ones when it is set
         self.potential_offset = None
         self._stag_coefs = None
         self._flags_base = 0

@@ -22,10 +22,13 @@ int32_t set_error(int32_t code, const char* fmt, ...) {
   return code;
 }
 
-static int32_t tile_shape(uint32_t flags, int32_t* tx, int32_t* ty) {
+static int32_t tile_shape(int32_t precision, uint32_t flags, int32_t* tx, int32_t* ty) {
   if (flags & FDS_FLAG_HAS_V) {
     *tx = 64;
     *ty = 16;
+    // double words: 64 x 12 stages 43 KB per CTA instead of 55 KB, which fits a
+    // fifth CTA per SM (lossless variants; measured 8 % faster on the 2048^2 step)
+    if (precision == FDS_PREC_DW && !(flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT))) *ty = 12;
   } else {
     *tx = 1024;
     *ty = 1;
@@ -52,11 +55,10 @@ int32_t fds_last_error(char* buf, size_t len) {
 int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, int32_t nx,
                             int32_t ny, int32_t* tile_x, int32_t* tile_y) {
   (void)family;
-  (void)precision;
   (void)nx;
   (void)ny;
   if (!tile_x || !tile_y) return fds::set_error(FDS_E_ARG, "null output pointer");
-  return fds::tile_shape(flags, tile_x, tile_y);
+  return fds::tile_shape(precision, flags, tile_x, tile_y);
 }
 
 int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, int32_t capacity) {
@@ -103,8 +105,8 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
   if ((prob->flags & FDS_FLAG_FLOW) &&
       (prob->family != FDS_FAMILY_ACOUSTIC || !has_v || (prob->flags & FDS_FLAG_AXI) ||
        !prob->flow_period || prob->precision == FDS_PREC_F32_T64))
-    return set_error(FDS_E_ARG, "flow needs a 2-D Cartesian float64/float32 acoustic field "
-                                "and its flow_period array");
+    return set_error(FDS_E_ARG, "flow needs a 2-D Cartesian float64/float32/double-word "
+                                "acoustic field and its flow_period array");
   const int ncomp = has_v ? 3 : 2;
   for (int k = 0; k < ncomp; ++k)
     if (!state->cur[k] || !state->nxt[k]) return set_error(FDS_E_ARG, "missing state buffer %d", k);
@@ -127,6 +129,9 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
     case FDS_PREC_F32_T64:
       if (prob->flags & FDS_FLAG_EXACT) return set_error(FDS_E_ARG, "exact mode is float64 only");
       return run_stag_f32t64(prob, state, tables, step0, nsteps, store_flux, s);
+    case FDS_PREC_DW:
+      if (prob->flags & FDS_FLAG_EXACT) return set_error(FDS_E_ARG, "exact mode is float64 only");
+      return run_stag_dw(prob, state, tables, step0, nsteps, store_flux, s);
     default:
       return set_error(FDS_E_ARG, "unknown precision %d", prob->precision);
   }
@@ -182,6 +187,8 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
     case FDS_PREC_F32_T64:
       return run_batch_f32t64(probs, states, tables, count, workspace, workspace_bytes, step0,
                               nsteps, store_flux, mode, s);
+    case FDS_PREC_DW:
+      return set_error(FDS_E_NOKERNEL, "batched runs are not built for double-word precision");
     default:
       return set_error(FDS_E_ARG, "unknown precision %d", p0.precision);
   }

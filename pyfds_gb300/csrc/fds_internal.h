@@ -12,7 +12,9 @@
 //   FDS_TILE_MENU:  shared-memory tiles (cells x, cells y, threads); slot layout 0
 //   FDS_MARCH_MENU: register-marching warps (cells per lane CX, rows TY, warps per
 //                   CTA); the tile is (32*CX - 2) x TY cells; slot layout 1
-#define FDS_TILE_MENU(X) X(64, 16, 256) X(32, 32, 256) X(128, 8, 256) X(64, 32, 512) X(128, 16, 512)
+#define FDS_TILE_MENU(X)                                                                   \
+  X(64, 16, 256) X(32, 32, 256) X(128, 8, 256) X(64, 32, 512) X(128, 16, 512) X(64, 12, 256) \
+  X(64, 8, 256)
 #define FDS_MARCH_MENU(X) X(2, 16, 4) X(2, 8, 4) X(2, 32, 4) X(1, 16, 4) X(1, 32, 4)
 
 namespace fds {
@@ -26,6 +28,8 @@ int32_t run_stag_f32(const FdsStagProblem*, FdsStagState*, const FdsStagTables*,
                      int32_t, int32_t, cudaStream_t);
 int32_t run_stag_f32t64(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int64_t,
                         int32_t, int32_t, cudaStream_t);
+int32_t run_stag_dw(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int64_t, int32_t,
+                    int32_t, cudaStream_t);
 
 int32_t run_batch_f64(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int32_t, void*,
                       size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);

@@ -63,6 +63,11 @@ int32_t launch_flow_shift(const FdsStagProblem* prob, void* const* cur, int64_t 
           (float*)cur[0], (float*)cur[1], (float*)cur[2], prob->nx, prob->ny, prob->flow_period,
           step);
       break;
+    case FDS_PREC_DW:  // double words move as 8-byte units (zero bits are 0 + 0)
+      flow_shift_kernel<unsigned long long, unsigned long long><<<prob->ny, 256, 0, stream>>>(
+          (unsigned long long*)cur[0], (unsigned long long*)cur[1], (unsigned long long*)cur[2],
+          prob->nx, prob->ny, prob->flow_period, step);
+      break;
     default:
       return set_error(FDS_E_ARG, "flow shift: precision %d not built", prob->precision);
   }

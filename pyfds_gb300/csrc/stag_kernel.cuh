@@ -38,6 +38,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "dw.cuh"
 #include "fds_capi.h"
 #include "tma.cuh"
 
@@ -102,12 +105,16 @@ __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
 // Resident CTAs per SM the 256-thread 2-D tile kernels are compiled for (the
 // register budget per thread follows: 65536 / (256 x blocks)). Measured on the
 // 2048^2 acoustic step: float64 potential 5 (4: -2 %, 6 spills and loses 6 %),
-// float32 potential 6 (4: -8 %).
+// float32 potential 6 (4: -8 %). Double words: 5 (the absorbing variants, 4, spill
+// at 5).
 #ifndef FDS_STAG_BLOCKS_256_F64
 #define FDS_STAG_BLOCKS_256_F64 5
 #endif
 #ifndef FDS_STAG_BLOCKS_256_F32
 #define FDS_STAG_BLOCKS_256_F32 6
+#endif
+#ifndef FDS_STAG_BLOCKS_256_DW
+#define FDS_STAG_BLOCKS_256_DW 5
 #endif
 #ifndef FDS_BATCH_BLOCKS_256
 #define FDS_BATCH_BLOCKS_256 4
@@ -136,18 +143,20 @@ struct StagCfg {
   static constexpr int MIN_BLOCKS =
       STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : FDS_BATCH_BLOCKS_256) : 2);
   // CTAs per SM of the single-field kernel for a potential of `psize` bytes per value
-  static constexpr int min_blocks(int psize) {
+  // (`dword`: double-word float32 pairs)
+  static constexpr int min_blocks(int psize, bool dword = false) {
     return STAGES == 2 ? 1
                        : (HAS_V ? (NT >= 512 ? 2
-                                             : (psize == 4 ? FDS_STAG_BLOCKS_256_F32
-                                                           : FDS_STAG_BLOCKS_256_F64))
+                                             : (dword ? (ABSORB ? 4 : FDS_STAG_BLOCKS_256_DW)
+                                                      : psize == 4 ? FDS_STAG_BLOCKS_256_F32
+                                                                   : FDS_STAG_BLOCKS_256_F64))
                                 : 2);
   }
 };
 
 template <typename T>
 __device__ __forceinline__ T ldg0(const T* p, int64_t i, int64_t n) {
-  return (i >= 0 && i < n) ? __ldg(p + i) : T(0);
+  return (i >= 0 && i < n) ? ldg_t(p + i) : T(0);
 }
 
 // Exact (reference-order) arithmetic: correctly rounded, never contracted.
@@ -157,6 +166,9 @@ __device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ dw xmul(const dw& a, const dw& b) { return a * b; }
+__device__ __forceinline__ dw xadd(const dw& a, const dw& b) { return a + b; }
+__device__ __forceinline__ dw xsub(const dw& a, const dw& b) { return a - b; }
 
 // Boundary chains of one component for this tile, applied to shared slots.
 // new = additive * old + value, additive as a number (pyfds/regions.py:125-145)
@@ -240,8 +252,8 @@ __device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* 
       if constexpr (C::ABSORB) r = xsub(r, absorb_term<C>(a, sF, pos, i));
       if constexpr (C::AXI && C::ABSORB && IS_X) {
         // + dt*mu/rho * vx / r**2   (pyfds/acoustics.py:213-215)
-        const TF rad = (TF)__ldg(a.rx + x);
-        const TF e = xmul((TF)__ldg(a.ex + i), u);
+        const TF rad = (TF)ldg_t(a.rx + x);
+        const TF e = xmul((TF)ldg_t(a.ex + i), u);
         r = xadd(r, e / xmul(rad, rad));
       }
       return xsub(u, r);
@@ -254,12 +266,13 @@ __device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* 
         // small gradients) and only the flux is rounded to float32
         const TP bp = (TP)sB[pos] * sP[pos];
         return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
-      } else if constexpr (sizeof(TF) == 4) {
-        // float32 temperature stored as T - offset: add the reference's interface
-        // term -(b - bm) * offset (zero inside a material, and when offset is 0)
-        return fma(-(b - bm), (TF)a.offset, fma(bm, pm, -(b * p)));
+      } else if constexpr (sizeof(TF) == 4 || std::is_same<TF, dw>::value) {
+        // float32 / double-word temperature stored as T - offset: add the reference's
+        // interface term -(b - bm) * offset (zero inside a material, and when offset
+        // is 0)
+        return settle(fma(-(b - bm), (TF)a.offset, fma(bm, pm, -(b * p))));
       } else {
-        return fma(bm, pm, -(b * p));
+        return settle(fma(bm, pm, -(b * p)));
       }
     } else {
       TF acc = sF[pos];
@@ -267,10 +280,10 @@ __device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* 
       acc = fma(bm, pm, acc);
       if constexpr (C::ABSORB) acc = absorb_fma<C>(a, sF, pos, i, acc);
       if constexpr (C::AXI && C::ABSORB && IS_X) {
-        const TF rad = (TF)__ldg(a.rx + x);
-        acc = acc - ((TF)__ldg(a.ex + i) * sF[pos]) / (rad * rad);
+        const TF rad = (TF)ldg_t(a.rx + x);
+        acc = acc - ((TF)ldg_t(a.ex + i) * sF[pos]) / (rad * rad);
       }
-      return acc;
+      return settle(acc);
     }
   }
 }
@@ -587,8 +600,8 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
           // a_p_vx.dot(vx * r): the flux is scaled by the radius of its column
           const int x = xo[k];
           const int xn = (x + 1 == a.nx) ? 0 : x + 1;
-          w = xmul(u, (TF)__ldg(a.rx + x));
-          wn = xmul(un1, (TF)__ldg(a.rx + xn));
+          w = xmul(u, (TF)ldg_t(a.rx + x));
+          wn = xmul(un1, (TF)ldg_t(a.rx + xn));
         }
         // forward difference, offsets [0, s]: (0 + (-k)*w) + kn*wn
         TF sx = xadd(-xmul(kxi, w), xmul(kxn, wn));
@@ -605,7 +618,7 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
           acc = fma(kyi, v, acc);
           acc = fma(-kyn, vn1, acc);
         }
-        pn[k] = (TP)acc;
+        pn[k] = (TP)settle(acc);
       } else {
         // float increment accumulated into a float64 potential
         TF inc = kxi * u;
@@ -642,7 +655,7 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
 // the current tile is computed from the other buffer. Staging is TMA when the
 // launch provides tensor maps (use_tma) and cp.async otherwise.
 template <class C, typename TP, typename TF, typename TC>
-__global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP)))
+__global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<TP, dw>::value))
     stag_step_kernel(const __grid_constant__ StagArgs<TP, TF, TC> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const bool iso = a.iso || !C::HAS_V;

@@ -163,7 +163,9 @@ StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, 
       return &launch_march<MarchCfg<CX, TY, NW, false>, TP, TF, TC>;                      \
     }                                                                                     \
   }
-  FDS_MARCH_MENU(FDS_PICK_MARCH)
+  if constexpr (!std::is_same<TP, dw>::value) {  // register marching shuffles scalars
+    FDS_MARCH_MENU(FDS_PICK_MARCH)
+  }
 #undef FDS_PICK_MARCH
   if constexpr (ALLOW_ACOUSTIC) {
     FDS_PICK(kTile1dX, 1, false, true, false, false, false)

@@ -84,10 +84,7 @@ class Animator:
         if eng is None or name not in eng.buffers or getattr(comp, '_where', 'host') == 'host':
             torch = require_cuda()
             return torch.as_tensor(np.asarray(comp.values, dtype=np.float64), device='cuda')
-        v = eng.buffers[name][0].to(dtype=require_cuda().float64)
-        if name == f._stag_components[0] and eng.offset:
-            v = v + eng.offset
-        return v
+        return eng.device_values(name)
 
     def show_setup(self, halt=True):
         raise NotImplementedError('plot windows need a graphics stack; this package records '

@@ -54,6 +54,11 @@ def test_struct_layouts_match_header():
 def test_tile_shapes(lib):
     assert _capi.tile_shape(0, 0, _capi.FLAG_HAS_V, 100, 100) == (64, 16)
     assert _capi.tile_shape(0, 0, 0, 1000, 1) == (1024, 1)
+    dw = _capi.PREC_DW
+    assert _capi.tile_shape(0, dw, _capi.FLAG_HAS_V, 100, 100) == (64, 12)
+    assert _capi.tile_shape(1, dw, _capi.FLAG_HAS_V | _capi.FLAG_AXI, 100, 100) == (64, 12)
+    assert _capi.tile_shape(0, dw, _capi.FLAG_HAS_V | _capi.FLAG_ABSORB, 100, 100) == (64, 16)
+    assert _capi.tile_shape(0, dw, 0, 1000, 1) == (1024, 1)
 
 
 def test_argument_errors_are_reported(lib):

@@ -247,7 +247,9 @@ def test_thermal_reduced_precision_error(gpu, precision, tol):
 
 
 MENU = [((64, 16), 1), ((32, 32), 1), ((128, 8), 1), ((64, 32), 1), ((128, 16), 1),
+        ((64, 12), 1), ((64, 8), 1),
         ((64, 16), 2), ((32, 32), 2), ((128, 8), 2), ((64, 32), 2), ((128, 16), 2),
+        ((64, 12), 2), ((64, 8), 2),
         ((62, 16), 1), ((62, 8), 1), ((62, 32), 1), ((30, 16), 1), ((30, 32), 1)]
 
 
