@@ -237,7 +237,8 @@ def run_batched(args):
     nt = int(specs[0]["steps"])
     fields = [workloads.build_field(sp, precision=args.precision) for sp in specs]
     cells = sum(f.num_points for f in fields)
-    tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else (64, 16)
+    tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else \
+        ((64, 12) if args.precision == "dw" else (64, 16))
     stages = args.stages or 1
     if args.autotune:
         from pyfds_gb300.autotune import autotune_batch
@@ -296,7 +297,7 @@ def run_batched(args):
         barrier()
         e2e_s = time.perf_counter() - t0
         e2e_value = ws * cells * nt / e2e_s / 1e9
-        esz = 8 if args.precision == "f64" else 4
+        esz = 8 if args.precision in ("f64", "dw") else 4
         h2d = sum(f.num_points * esz * 5 for f in fields) + sum(
             int(p["tabs"]["blob"].numel()) for p in r.plans) + int(r.workspace.numel())
         d2h = sum(sum(o.numel() * 8 for o in p["outs"] if o is not None) for p in r.plans) + \
@@ -309,7 +310,8 @@ def run_batched(args):
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": args.precision, "data": "synthetic (seeded layered media, no dataset)",
+            "dtype": {"dw": "f32x2 (double-word)"}.get(args.precision, args.precision),
+            "data": "synthetic (seeded layered media, no dataset)",
             "config": {"workload": "batched: %d layered-media Acoustic2D instances, n in "
                                    "[128, 1024] log-uniform, %d steps each" % (len(fields), nt),
                        "cells": cells, "time_steps_per_step": nt, "precision": args.precision,
@@ -317,7 +319,8 @@ def run_batched(args):
                        "launch": "one kernel per time step for all instances, whole run "
                                  "replayed from one CUDA graph",
                        "l2": "inputs larger than L2 (%.0f MB of state)"
-                             % (cells * 6 * (8 if args.precision == "f64" else 4) / 2 ** 20),
+                             % (cells * 6 * (8 if args.precision in ("f64", "dw") else 4)
+                                / 2 ** 20),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

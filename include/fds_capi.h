@@ -53,8 +53,7 @@ extern "C" {
 #define FDS_PREC_DW 3      /* double-word: every state and coefficient value is a pair of
                               float32 {hi, lo} (8 bytes, value hi + lo, |lo| <= ulp(hi)/2)
                               computed with compensated float32 arithmetic (48-bit
-                              significands); no register-marching tiles, not batched,
-                              not exact */
+                              significands); no register-marching tiles, not exact */
 
 /* FdsStagProblem.flags */
 #define FDS_FLAG_HAS_V 1u   /* second flux component (2-D fields) */

@@ -18,7 +18,7 @@ class StagField:
                  float32 fluxes with a float64 temperature) or "dw" (double-word:
                  every value a float32 pair hi + lo with 48-bit significands,
                  compensated float32 arithmetic; float64-class accuracy on the FP32
-                 pipe; not batched). Thermal "f32" stores the temperature as a
+                 pipe). Thermal "f32" stores the temperature as a
                  deviation from ``potential_offset`` (default: the mean initial
                  temperature); thermal "dw" does so when ``potential_offset`` is set.
       exact:     float64 only; evaluate in the reference's operation order without

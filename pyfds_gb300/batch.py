@@ -30,8 +30,6 @@ class BatchRunner:
         for f in self.fields:
             if type(f) is not type(f0) or f.precision != f0.precision:
                 raise ValueError("batched fields must share class and precision")
-            if f.precision == "dw":
-                raise ValueError("batched runs are not built for precision='dw'")
             if f.step != f0.step:
                 raise ValueError("batched fields must stand at the same step")
             if tile is not None:

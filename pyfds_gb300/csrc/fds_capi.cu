@@ -188,7 +188,8 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
       return run_batch_f32t64(probs, states, tables, count, workspace, workspace_bytes, step0,
                               nsteps, store_flux, mode, s);
     case FDS_PREC_DW:
-      return set_error(FDS_E_NOKERNEL, "batched runs are not built for double-word precision");
+      return run_batch_dw(probs, states, tables, count, workspace, workspace_bytes, step0, nsteps,
+                          store_flux, mode, s);
     default:
       return set_error(FDS_E_ARG, "unknown precision %d", p0.precision);
   }

@@ -35,6 +35,8 @@ int32_t run_batch_f64(const FdsStagProblem*, FdsStagState*, const FdsStagTables*
                       size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);
 int32_t run_batch_f32(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int32_t, void*,
                       size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);
+int32_t run_batch_dw(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int32_t, void*,
+                     size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);
 int32_t run_batch_f32t64(const FdsStagProblem*, FdsStagState*, const FdsStagTables*, int32_t,
                          void*, size_t, int64_t, int32_t, int32_t, uint32_t, cudaStream_t);
 size_t batch_workspace_bytes(int32_t count, int64_t total_tiles);

@@ -9,4 +9,10 @@ int32_t run_stag_dw(const FdsStagProblem* p, FdsStagState* s, const FdsStagTable
                     int64_t step0, int32_t nsteps, int32_t store_flux, cudaStream_t st) {
   return run_stag_typed<dw, dw, dw, false, true>(p, s, t, step0, nsteps, store_flux, st);
 }
+int32_t run_batch_dw(const FdsStagProblem* p, FdsStagState* s, const FdsStagTables* t,
+                     int32_t count, void* ws, size_t wsb, int64_t step0, int32_t nsteps,
+                     int32_t store_flux, uint32_t mode, cudaStream_t st) {
+  return run_batch_typed<dw, dw, dw, true>(p, s, t, count, ws, wsb, step0, nsteps, store_flux,
+                                           mode, st);
+}
 }  // namespace fds

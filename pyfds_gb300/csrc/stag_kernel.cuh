@@ -79,6 +79,7 @@ struct StagCore {
   int32_t iso;  // by == bx and ky == kx: the y factors are not staged separately
   int32_t ntiles;
   int32_t use_tma;  // stage the region with TMA boxes (tm[]) instead of cp.async
+  int32_t prefetch; // TMA path: also prefetch into L2 the region of tile + prefetch (0: off)
   int32_t* status;  // OR-ed with kStatus* bits; may be null
   double offset;    // potential stored as value - offset (thermal float32), else 0
 };
@@ -433,6 +434,27 @@ __device__ __forceinline__ void tma_issue_tile(const StagCore<TP, TF, TC>& a, co
   }
 }
 
+// L2 prefetch of the boxes of a later tile (one thread), when they lie inside the
+// arrays: the CTA that stages that tile then reads L2 instead of waiting on DRAM.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void tma_prefetch_tile(const StagCore<TP, TF, TC>& a,
+                                                  const CUtensorMap* tm, int tile, bool iso) {
+  const int gx = (tile % a.tiles_x) * C::TX - C::OX;
+  const int gy = (tile / a.tiles_x) * C::TY - C::OY;
+  if (gx < 0 || gy < 0 || gx + C::RX > a.nx || gy + C::RY > a.ny) return;
+  tma_prefetch_2d(&tm[0], gx, gy);
+  if constexpr (C::MEMORY) {
+    tma_prefetch_2d(&tm[1], gx, gy);
+    if constexpr (C::HAS_V) tma_prefetch_2d(&tm[2], gx, gy);
+  }
+  tma_prefetch_2d(&tm[3], gx, gy);
+  tma_prefetch_2d(&tm[4], gx, gy);
+  if (!iso) {
+    tma_prefetch_2d(&tm[5], gx, gy);
+    tma_prefetch_2d(&tm[6], gx, gy);
+  }
+}
+
 // Waits (bounded) for a tile's boxes, then patches the slots whose column lies
 // outside [0, nx): the box reads them as zeros, the flat-index semantics want the
 // cells of the neighbouring row. Returns false for every thread on a timeout.
@@ -670,7 +692,11 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
   __syncthreads();
   if constexpr (C::STAGES == 1) {
     if (tma) {
-      if (threadIdx.x == 0) tma_issue_tile<C>(a, a.tm, t, buf0, iso, bars);
+      if (threadIdx.x == 0) {
+        tma_issue_tile<C>(a, a.tm, t, buf0, iso, bars);
+        if (a.prefetch > 0 && t + a.prefetch < a.ntiles)
+          tma_prefetch_tile<C>(a, a.tm, t + a.prefetch, iso);
+      }
       if (!tma_finish_tile<C>(a, t, buf0, iso, bars, 0)) return;
     } else {
       stage_tile<C>(a, t, buf0, iso);

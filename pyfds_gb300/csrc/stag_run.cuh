@@ -100,16 +100,18 @@ int32_t launch_stag(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
     attr_bytes = smem;
   }
   select_tma<C>(a, tc, tc ? tc->state : nullptr);
-  int grid = a.ntiles;
-  if (C::STAGES > 1) {
-    int& o = occ[iso ? 1 : 0];
-    if (o < 0) {
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &o, stag_step_kernel<C, TP, TF, TC>, C::NT, smem);
-      if (e != cudaSuccess || o < 1) o = 1;
-    }
-    grid = a.ntiles < o * nsm ? a.ntiles : o * nsm;
+  int& o = occ[iso ? 1 : 0];
+  if (o < 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &o, stag_step_kernel<C, TP, TF, TC>, C::NT, smem);
+    if (e != cudaSuccess || o < 1) o = 1;
   }
+  int grid = a.ntiles;
+  if (C::STAGES > 1) grid = a.ntiles < o * nsm ? a.ntiles : o * nsm;
+  // one-stage TMA path: each CTA prefetches into L2 the region of the tile 0.4 waves
+  // of resident CTAs ahead (measured on the 2048^2 step against 0 to 2 waves:
+  // double words +6 %, float32 +5 %, float64 +1 %; two waves already lose)
+  a.prefetch = (C::STAGES == 1 && a.use_tma) ? (int32_t)(0.4 * o * nsm) : 0;
   stag_step_kernel<C, TP, TF, TC><<<grid, C::NT, smem, s>>>(a);
   return FDS_OK;
 }

@@ -42,6 +42,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// L2 prefetch of one 2-D box of `map` at (x, y): a hint, with no shared-memory
+// destination and no completion. Callers pass boxes inside the array.
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];\n" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y)
+               : "memory");
+}
+
 // Waits for phase `parity` of the barrier to complete; gives up after `limit`
 // polls (each poll may suspend the thread for a short hardware-defined time).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {

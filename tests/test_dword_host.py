@@ -1,6 +1,6 @@
 """Host side of the double-word precision (precision="dw"), without a GPU: the
-float64 <-> (hi, lo) float32 split, the ABI constant, and the argument checks of
-the C ABI that reject what the mode does not cover."""
+float64 <-> (hi, lo) float32 split, the ABI constant, the argument check of the C
+ABI that rejects exact double words, and the temperature-offset policy."""
 import ctypes as C
 import os
 import re
@@ -62,20 +62,13 @@ def _fake_problem(precision, flags):
     return pr, st
 
 
-def test_abi_rejects_exact_and_batched_double_words():
+def test_abi_rejects_exact_double_words():
     lib = _capi.load()
     tb = _capi.FdsStagTables()
     pr, st = _fake_problem(_capi.PREC_DW, _capi.FLAG_HAS_V | _capi.FLAG_EXACT)
     assert lib.fds_stag_run(C.byref(pr), C.byref(st), C.byref(tb), 0, 1, 1, None) == \
         _capi.FDS_E_ARG
     assert "float64 only" in _capi.last_error()
-    pr, st = _fake_problem(_capi.PREC_DW, _capi.FLAG_HAS_V)
-    ws = (C.c_uint8 * 512)()
-    base = (C.addressof(ws) + 255) // 256 * 256
-    code = lib.fds_stag_batch_run(C.byref(pr), C.byref(st), C.byref(tb), 1, C.c_void_p(base), 256,
-                                  0, 1, 1, 3, None)
-    assert code == _capi.FDS_E_NOKERNEL
-    assert "double-word" in _capi.last_error()
 
 
 @pytest.mark.parametrize("precision,explicit,expected", [
