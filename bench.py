@@ -608,12 +608,85 @@ def run_surrogate_iter(args):
     return 0
 
 
+# workloads whose float64 line also times the double-word step (same field, same box)
+DW_WORKLOADS = ("acoustic2d", "acoustic1d", "axi", "thermal")
+
+
+def _reset_state(field, eng, spec, dev):
+    """Zero the device state of a field and load the workload's initial values."""
+    import torch
+    from pyfds_gb300._engine import split_dw
+    for name in field._stag_components:
+        for t in eng.buffers[name]:
+            t.zero_()
+        if name in (spec.get("init") or {}):
+            v = np.asarray(spec["init"][name], dtype=np.float64).reshape(-1)
+            if field.precision == "dw":
+                v = split_dw(v)
+            eng.buffers[name][0].copy_(torch.as_tensor(v, device=dev,
+                                                       dtype=eng.buffers[name][0].dtype))
+
+
+def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
+    """The same workload in double-word precision: throughput (same timing as the
+    float64 line), its step kernel's launch time and HBM fraction, and the error of
+    its outputs against the float64 outputs of this run (relative L2 per output the
+    wave reached, i.e. norm >= 1e-6 of the largest; the others by absolute error
+    relative to the largest output's norm)."""
+    import torch
+    from pyfds_gb300 import workloads
+    f = workloads.build_field(spec, precision="dw")
+    f.assemble_matrices()
+    eng = f._engine()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    plan = eng.prepare(0, nt)
+    for _ in range(args.warmup):
+        _reset_state(f, eng, spec, dev)
+        eng.launch(plan)
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    for _ in range(args.steps):
+        _reset_state(f, eng, spec, dev)
+        eng.launch(plan)
+    ev[1].record(stream)
+    barrier()
+    ms = ev[0].elapsed_time(ev[1]) / args.steps
+    _reset_state(f, eng, spec, dev)
+    ev[2].record(stream)
+    eng.launch(plan)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    launch_ms = ev[2].elapsed_time(ev[3]) / nt
+    rows = [r for o in plan["outs"] if o is not None for r in o.cpu().numpy().T]
+    refs = [r for o in ref_outs if o is not None for r in o.T]
+    top = max((float(np.linalg.norm(r)) for r in refs), default=0.0)
+    worst, unreached, worst_abs = 0.0, 0, 0.0
+    for a, b in zip(rows, refs):
+        nb = float(np.linalg.norm(b))
+        if nb >= 1e-6 * top and nb > 0:
+            worst = max(worst, float(np.linalg.norm(a - b)) / nb)
+        else:
+            unreached += 1
+            worst_abs = max(worst_abs, float(np.linalg.norm(a - b)) / top if top else 0.0)
+    cells = f.num_points
+    peak, _ = _peaks()
+    achieved = cells * bytes_per_cell / (launch_ms * 1e-3) / 1e9 if bytes_per_cell else None
+    geo = eng._geometry()
+    return {"value": cells * nt / (ms * 1e-3) / 1e9, "unit": "Gcell/s", "ms_per_step": ms,
+            "dtype": "f32x2 (double-word)", "tile": "%dx%d" % (geo.tx, geo.ty),
+            "launch_ms": launch_ms, "achieved_gbs": achieved,
+            "hbm_frac": achieved / peak if achieved and peak else None,
+            "max_rel_l2_vs_f64": worst, "unreached_outputs": unreached,
+            "unreached_max_abs_vs_largest": worst_abs}
+
+
 def run_ours(args):
     import torch
     ws, rank, local = _init_replicas()
     dev = torch.device("cuda", torch.cuda.current_device())
     from pyfds_gb300 import workloads, _capi
-    from pyfds_gb300._engine import split_dw
     builder, kwargs, balg = WORKLOADS[args.workload]
     kwargs = dict(kwargs)
     if args.time_steps:
@@ -634,15 +707,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def zero_state():
-        for name in field._stag_components:
-            for t in eng.buffers[name]:
-                t.zero_()
-            if name in (spec.get("init") or {}):
-                v = np.asarray(spec["init"][name], dtype=np.float64).reshape(-1)
-                if args.precision == "dw":
-                    v = split_dw(v)
-                eng.buffers[name][0].copy_(torch.as_tensor(v, device=dev,
-                                                           dtype=eng.buffers[name][0].dtype))
+        _reset_state(field, eng, spec, dev)
 
     plan = eng.prepare(0, nt)
     for _ in range(args.warmup):
@@ -670,6 +735,10 @@ def run_ours(args):
     ev3.record(stream)
     torch.cuda.synchronize()
     launch_ms = ev2.elapsed_time(ev3) / nt
+    ref_outs = [o.cpu().numpy() if o is not None else None for o in plan["outs"]]
+    dword = None
+    if args.precision == "f64" and not args.no_dw and args.workload in DW_WORKLOADS:
+        dword = _double_word_leg(args, spec, nt, ref_outs, barrier, balg.get("dw"))
     # ---------------- e2e through the public API with host buffers
     e2e_steps = 0 if args.no_e2e else max(1, args.steps)
     host_init = {name: np.zeros(cells) for name in field._stag_components}
@@ -738,6 +807,8 @@ def run_ours(args):
             # moving medium, the row shift and the next step's pressure bounds)
             "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else
                                               1 if args.workload == "nonlinear1d" else nt + 1))}
+    if dword is not None:
+        line["double_word"] = dword
     dfma = _traffic_from_profiles("%s_%s" % (args.workload, args.precision), "dfma_per_launch")
     if dfma and launch_ms:
         # the FP64 pipe bounds the float64 step: its roofline beside the HBM one. Peak =
@@ -775,6 +846,9 @@ def main():
     ap.add_argument("--precision", choices=["f64", "f32", "f32_t64", "dw"], default="f64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling)")
+    ap.add_argument("--no-dw", action="store_true",
+                    help="float64 lines: skip the double-word leg (the same workload in "
+                         "precision='dw')")
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
     ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2],
                     help="staging buffers per CTA (0: automatic)")
