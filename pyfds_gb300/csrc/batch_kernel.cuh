@@ -5,7 +5,8 @@
 // ping-pong parity: parity 0 reads `cur` and writes `nxt`, parity 1 the reverse),
 // holding its grid, coefficient pointers, tables and the TMA tensor maps of the
 // arrays it reads. A work list of (instance, tile) pairs covers every tile of
-// every instance. STAGES == 1: one CTA per work item. STAGES == 2: persistent
+// every instance. STAGES == 1: one CTA per work item, which also prefetches into
+// L2 the region of the item `prefetch` places ahead. STAGES == 2: persistent
 // CTAs walk the work list, prefetching the next item's region (possibly another
 // instance's) while computing the current one.
 #pragma once
@@ -36,7 +37,7 @@ __host__ __device__ constexpr size_t batch_smem_bytes() {
 template <class C, typename TP, typename TF, typename TC>
 __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     stag_batch_kernel(const StagArgs<TP, TF, TC>* __restrict__ descs, const int2* __restrict__ work,
-                      int nwork, const StepInfo si, int parity) {
+                      int nwork, const StepInfo si, int parity, int prefetch) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(false);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + C::STAGES * bytes);
@@ -56,7 +57,15 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     const bool iso = a.iso || !C::HAS_V;
     const StagBuf<TP, TF, TC> buf = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
     if (a.use_tma && aligned) {
-      if (threadIdx.x == 0) tma_issue_tile<C>(a, d->tm, it.y, buf, iso, bars);
+      if (threadIdx.x == 0) {
+        tma_issue_tile<C>(a, d->tm, it.y, buf, iso, bars);
+        // L2 prefetch of the work item `prefetch` ahead (possibly another instance)
+        if (prefetch > 0 && w + prefetch < nwork) {
+          const int2 ip = work[w + prefetch];
+          const StagArgs<TP, TF, TC>* dp = descs + 2 * ip.x + parity;
+          if (dp->use_tma) tma_prefetch_tile<C>(*dp, dp->tm, ip.y, dp->iso || !C::HAS_V);
+        }
+      }
       if (!tma_finish_tile<C>(a, it.y, buf, iso, bars, 0)) return;
     } else {
       stage_tile<C>(a, it.y, buf, iso);

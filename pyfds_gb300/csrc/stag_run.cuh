@@ -397,15 +397,16 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
     attr = smem;
   }
-  int grid = (int)nwork;
-  if (C::STAGES > 1) {
-    if (occ < 0) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stag_batch_kernel<C, TP, TF, TC>,
-                                                        C::NT, smem);
-      if (e != cudaSuccess || occ < 1) occ = 1;
-    }
-    grid = (int)std::min<int64_t>(nwork, (int64_t)occ * nsm);
+  if (occ < 0) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stag_batch_kernel<C, TP, TF, TC>,
+                                                      C::NT, smem);
+    if (e != cudaSuccess || occ < 1) occ = 1;
   }
+  int grid = (int)nwork;
+  if (C::STAGES > 1) grid = (int)std::min<int64_t>(nwork, (int64_t)occ * nsm);
+  // one-stage: prefetch the work item 0.4 waves of resident CTAs ahead (as the
+  // single-field kernel)
+  const int prefetch = C::STAGES == 1 ? (int)(0.4 * occ * nsm) : 0;
   if (nsteps > 0) {
     stag_batch_prologue_kernel<TP, TF, TC><<<count, 256, 0, stream>>>(d_desc, count, step0);
     e = cudaGetLastError();
@@ -415,7 +416,7 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     const StepInfo si{step0 + s, step0, (s + 1 < nsteps) ? 1 : 0,
                       (store_flux || s + 1 == nsteps) ? 1 : 0};
     stag_batch_kernel<C, TP, TF, TC><<<grid, C::NT, smem, stream>>>(d_desc, d_work, (int)nwork, si,
-                                                                    s & 1);
+                                                                    s & 1, prefetch);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch step: %s", cudaGetErrorString(e));
   }
