@@ -658,11 +658,13 @@ def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
     eng.launch(plan)
     ev[3].record(stream)
     torch.cuda.synchronize()
-    launch_ms = ev[2].elapsed_time(ev[3]) / nt
+    step_kernel_ms = ev[2].elapsed_time(ev[3]) / nt  # per time step
+    spl = 2 if eng.stages() == 3 else 1  # steps per launch
     rows = [r for o in plan["outs"] if o is not None for r in o.cpu().numpy().T]
     refs = [r for o in ref_outs if o is not None for r in o.T]
     top = max((float(np.linalg.norm(r)) for r in refs), default=0.0)
     worst, unreached, worst_abs = 0.0, 0, 0.0
+    nonfinite = sum(int(not np.all(np.isfinite(a))) for a in rows)
     for a, b in zip(rows, refs):
         nb = float(np.linalg.norm(b))
         if nb >= 1e-6 * top and nb > 0:
@@ -670,16 +672,18 @@ def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
         else:
             unreached += 1
             worst_abs = max(worst_abs, float(np.linalg.norm(a - b)) / top if top else 0.0)
+    if nonfinite:  # never report a NaN comparison as agreement
+        worst = worst_abs = None
     cells = f.num_points
     peak, _ = _peaks()
-    achieved = cells * bytes_per_cell / (launch_ms * 1e-3) / 1e9 if bytes_per_cell else None
+    achieved = cells * bytes_per_cell / (step_kernel_ms * 1e-3) / 1e9 if bytes_per_cell else None
     geo = eng._geometry()
     return {"value": cells * nt / (ms * 1e-3) / 1e9, "unit": "Gcell/s", "ms_per_step": ms,
             "dtype": "f32x2 (double-word)", "tile": "%dx%d" % (geo.tx, geo.ty),
-            "launch_ms": launch_ms, "achieved_gbs": achieved,
+            "launch_ms": step_kernel_ms * spl, "steps_per_launch": spl, "achieved_gbs": achieved,
             "hbm_frac": achieved / peak if achieved and peak else None,
             "max_rel_l2_vs_f64": worst, "unreached_outputs": unreached,
-            "unreached_max_abs_vs_largest": worst_abs}
+            "unreached_max_abs_vs_largest": worst_abs, "nonfinite_outputs": nonfinite}
 
 
 def run_ours(args):
@@ -734,7 +738,10 @@ def run_ours(args):
     eng.launch(plan)
     ev3.record(stream)
     torch.cuda.synchronize()
-    launch_ms = ev2.elapsed_time(ev3) / nt
+    # time per step of the step kernel (two steps per launch with stages 3)
+    step_kernel_ms = ev2.elapsed_time(ev3) / nt
+    spl = 2 if eng.stages() == 3 else 1  # steps per launch
+    launch_ms = step_kernel_ms * spl
     ref_outs = [o.cpu().numpy() if o is not None else None for o in plan["outs"]]
     dword = None
     if args.precision == "f64" and not args.no_dw and args.workload in DW_WORKLOADS:
@@ -776,8 +783,12 @@ def run_ours(args):
         return 0
     peak, peak_kind = _peaks()
     bpc = balg.get(args.precision)
-    achieved = cells * bpc / (launch_ms * 1e-3) / 1e9 if bpc else None
-    traffic = _traffic_from_profiles("%s_%s" % (args.workload, args.precision))
+    # algorithmic bytes per cell update (one read and one write of the state, one read
+    # of the coefficients per step) over the time per step; with two steps per launch
+    # the kernel moves about half of that from DRAM (see "traffic", per launch)
+    achieved = cells * bpc / (step_kernel_ms * 1e-3) / 1e9 if bpc else None
+    pkey = "%s_%s%s" % (args.workload, args.precision, "_tb2" if spl == 2 else "")
+    traffic = _traffic_from_profiles(pkey)
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -787,7 +798,7 @@ def run_ours(args):
             "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
                        "precision": args.precision, "tile": "%dx%d" % (eng._geometry().tx, eng._geometry().ty),
-                       "stages": args.stages,
+                       "stages": eng.stages(),
                        "l2": "inputs larger than L2 (working set %.0f MB > %.0f MB)"
                              % ((state_bytes * 2 + coef_bytes) / 2 ** 20, L2_BYTES / 2 ** 20),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -800,16 +811,19 @@ def run_ours(args):
                                             "per step",
                                     "nonlinear1d": "nl1d_kernel (every step in one launch; the "
                                                    "field stays in L1/L2)"}.get(
-                                        args.workload, "stag_step_kernel"),
-                         "bytes_per_cell": bpc, "launch_ms": launch_ms},
+                                        args.workload,
+                                        "stag_tb2_kernel" if spl == 2 else "stag_step_kernel"),
+                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl},
             "clocks": clk.summary(),
-            # per simulate(): a prologue, then per step the step kernel (and, for a
-            # moving medium, the row shift and the next step's pressure bounds)
+            # per simulate(): a prologue, then per step (per two steps with stages 3)
+            # the step kernel (and, for a moving medium, the row shift and the next
+            # step's pressure bounds)
             "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else
-                                              1 if args.workload == "nonlinear1d" else nt + 1))}
+                                              1 if args.workload == "nonlinear1d" else
+                                              (nt + spl - 1) // spl + 1))}
     if dword is not None:
         line["double_word"] = dword
-    dfma = _traffic_from_profiles("%s_%s" % (args.workload, args.precision), "dfma_per_launch")
+    dfma = _traffic_from_profiles(pkey, "dfma_per_launch")
     if dfma and launch_ms:
         # the FP64 pipe bounds the float64 step: its roofline beside the HBM one. Peak =
         # 2 DFMA per clock per SM (ncu's peak_sustained of the DFMA counter) x SMs x the
@@ -850,7 +864,7 @@ def main():
                     help="float64 lines: skip the double-word leg (the same workload in "
                          "precision='dw')")
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
-    ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2, 3],
                     help="staging buffers per CTA (0: automatic)")
     ap.add_argument("--batch", type=int, default=0, help="instances of the batched workload")
     ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")

@@ -114,7 +114,10 @@ typedef struct FdsStagProblem {
   int32_t tile_y; /* fds_stag_tile_shape, or for lossless 2-D non-exact variants any
                      shape listed by fds_stag_tile_menu */
   int32_t stages; /* 0 (automatic) or 1: one CTA per tile; 2: persistent CTAs that
-                     prefetch the next tile while computing one (lossless 2-D variants) */
+                     prefetch the next tile while computing one (lossless 2-D variants);
+                     3: two steps per tile and launch (lossless 2-D, non-exact, no
+                     moving medium, not float32-with-float64-potential; tables in slot
+                     layout 2, see fds_stag_tile_menu) */
   FdsCoefs coefs;
   double offset;  /* thermal float32 only: the temperature is stored as T - offset
                      (finer float spacing near a reference temperature); the flux
@@ -151,13 +154,16 @@ typedef struct FdsBoundOp {
 } FdsBoundOp;
 
 /* One boundary cell of one tile: the chain ops[op_begin, op_end) applied in order
- * to the tile's shared-memory slot `pos`; `cell` is the flat index. 24 bytes. */
+ * to the tile's shared-memory slot `pos`; `cell` is the flat index. A cell can sit
+ * in several tiles' slots (halos that a tile recomputes); `primary` is 1 for one of
+ * them (the owning tile's), and the first-step prologue, which works on the global
+ * array, applies only primary groups. 24 bytes. */
 typedef struct FdsBoundGroup {
   int64_t cell;
   int32_t pos;
   int32_t op_begin;
   int32_t op_end;
-  int32_t pad;
+  int32_t primary;
 } FdsBoundGroup;
 
 /* One output sample slot: column `col` of the component's output buffer reads
@@ -211,7 +217,12 @@ int32_t fds_stag_tile_shape(int32_t family, int32_t precision, uint32_t flags, i
  *   0 (shared-memory tile): pos = (ly + 1) * (tile_x + 8) + lx + 4   (1-D: ly + 0)
  *   1 (register marching):  pos = ly * (tile_x + 2) + lx + 1
  * with (lx, ly) the cell relative to the tile's first owned cell. (New: no
- * reference counterpart; tiling is a property of the GPU kernel.) */
+ * reference counterpart; tiling is a property of the GPU kernel.)
+ * Two steps per tile (FdsStagProblem.stages = 3; tiles 64x16, 64x12, 64x8, 32x32)
+ * use layout 2: pos = (ly + 2) * (tile_x + 8) + lx + 4, and a tile's bound groups
+ * cover every slot of the ring it computes in its first step (potential: lx in
+ * -1 .. tile_x, ly in -1 .. tile_y; x flux: lx up to tile_x + 1; y flux: ly up to
+ * tile_y + 1), each cell once per flat-index alias, one placement flagged primary. */
 int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, int32_t capacity);
 
 /*

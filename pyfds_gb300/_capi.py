@@ -29,6 +29,10 @@ PREC_F32 = 1
 PREC_F32_T64 = 2
 PREC_DW = 3
 
+# tiles built for two steps per tile (FdsStagProblem.stages = 3; FDS_TB2_MENU in
+# csrc/fds_internal.h)
+TWO_STEP_TILES = ((64, 16), (64, 12), (64, 8), (32, 32))
+
 FLAG_HAS_V = 1
 FLAG_ABSORB = 2
 FLAG_AXI = 4
@@ -97,7 +101,7 @@ BATCH_STATIC_MAX_BYTES = 8 << 20
 BOUND_OP_DTYPE = np.dtype([("scalar", "<f8"), ("mul", "<f8"), ("off", "<i8"),
                            ("stride", "<i4"), ("flags", "<i4")], align=True)
 BOUND_GROUP_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("op_begin", "<i4"),
-                              ("op_end", "<i4"), ("pad", "<i4")], align=True)
+                              ("op_end", "<i4"), ("primary", "<i4")], align=True)
 PROBE_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("col", "<i4")], align=True)
 assert BOUND_OP_DTYPE.itemsize == 32
 assert BOUND_GROUP_DTYPE.itemsize == 24

@@ -214,8 +214,33 @@ class StagEngine:
             v += self.offset
         return v
 
-    # ------------------------------------------------------------------ tables
-    def _geometry(self):
+    # ------------------------------------------------------------------ stages
+    # precisions and families where two steps per tile are the faster default
+    # (measured on the 2048^2 and axisymmetric steps: float32 +26 %, double words
+    # +7 %; double-word thermal fields lose 10 % and keep one step)
+    TWO_STEP_AUTO = {("f32", _capi.FAMILY_ACOUSTIC), ("f32", _capi.FAMILY_THERMAL),
+                     ("dw", _capi.FAMILY_ACOUSTIC)}
+
+    def stages(self, batched=False):
+        """FdsStagProblem.stages of the next launch: the field's ``stages`` when set;
+        for 0 (automatic) two steps per tile (3) where that is the faster default and
+        the variant has a two-step kernel (lossless 2-D, not exact, no moving medium,
+        a two-step tile), else 0. Batched runs take 0, 1 or 2."""
+        f = self.field
+        st = int(getattr(f, "stages", 0) or 0)
+        if batched:
+            return st if st in (1, 2) else 0
+        if st:
+            return st
+        flags = f._stag_flags()
+        lossless_2d = (flags & _capi.FLAG_HAS_V) and not (
+            flags & (_capi.FLAG_ABSORB | _capi.FLAG_EXACT | _capi.FLAG_FLOW))
+        if lossless_2d and (f.precision, f._stag_family) in self.TWO_STEP_AUTO:
+            if self._tile_shape() in _capi.TWO_STEP_TILES:
+                return 3
+        return 0
+
+    def _tile_shape(self):
         f = self.field
         prec = PRECISIONS[f.precision]
         flags = f._stag_flags()
@@ -223,7 +248,16 @@ class StagEngine:
         tile = getattr(f, "tile", None)
         if tile is not None and (flags & _capi.FLAG_HAS_V):
             tx, ty = int(tile[0]), int(tile[1])
+        return tx, ty
+
+    # ------------------------------------------------------------------ tables
+    def _geometry(self, batched=False):
+        f = self.field
+        flags = f._stag_flags()
+        tx, ty = self._tile_shape()
         layout = _capi.tile_layout(tx, ty) if (flags & _capi.FLAG_HAS_V) else 0
+        if self.stages(batched) == 3:
+            layout = 2  # two steps per tile
         return _tables.TileGeometry(f._nx, f._ny, tx, ty, (flags & _capi.FLAG_HAS_V) != 0,
                                     layout)
 
@@ -292,7 +326,7 @@ class StagEngine:
         return st
 
     # --------------------------------------------------------------------- run
-    def prepare(self, step0, nsteps, cache_tables=False):
+    def prepare(self, step0, nsteps, cache_tables=False, batched=False):
         """Upload what the host changed and compile the tables for steps
         ``step0 .. step0+nsteps-1``; returns a launch plan for ``launch``."""
         torch = require_cuda()
@@ -300,10 +334,11 @@ class StagEngine:
         dev = torch.device("cuda", torch.cuda.current_device())
         self._upload_coefs(torch, dev)
         self._sync_state_to_device(torch, dev)
-        geo = self._geometry()
+        geo = self._geometry(batched)
         step_end = step0 + nsteps
         if cache_tables:
-            fp = self._fingerprint()
+            # the tables depend on the tiling too (tile shape, slot layout)
+            fp = (self._fingerprint(), geo.tx, geo.ty, geo.layout)
             if self.table_cache is not None and self.table_cache[0] == fp and \
                     self.table_cache[2] >= step_end:
                 tabs = self.table_cache[1]
@@ -322,7 +357,7 @@ class StagEngine:
         prob.ny = f._ny
         prob.tile_x = geo.tx
         prob.tile_y = geo.ty
-        prob.stages = int(getattr(f, "stages", 0) or 0)
+        prob.stages = self.stages(batched)
         prob.offset = self._potential_offset()
         for name in ("bx", "by", "kx", "ky", "aym", "axm", "ad", "axp", "ayp", "ex", "rx"):
             t = self.coef_tensors.get(name)

@@ -26,7 +26,13 @@ ROLE_POTENTIAL, ROLE_UX, ROLE_VY = 0, 1, 2
 
 class TileGeometry:
     """Tiling used by the kernel: ``tx`` x ``ty`` owned cells per tile, and how a
-    tile numbers its slots (layout 0: stag_kernel.cuh, layout 1: march_kernel.cuh)."""
+    tile numbers its slots (layout 0: the one-step tile kernel, layout 1: the
+    register-marching kernel, layout 2: the two-step tile kernel; stag_kernel.cuh,
+    march_kernel.cuh)."""
+
+    # layout 2: margins (left, right, above, below) of the ring on which a tile
+    # computes each component in its first step (the second step computes a subset)
+    RING = {ROLE_POTENTIAL: (1, 1, 1, 1), ROLE_UX: (1, 2, 1, 1), ROLE_VY: (1, 1, 1, 2)}
 
     def __init__(self, nx, ny, tx, ty, has_v, layout=0):
         self.nx, self.ny, self.tx, self.ty = int(nx), int(ny), int(tx), int(ty)
@@ -38,6 +44,11 @@ class TileGeometry:
         if self.layout == 0:
             # shared-memory region: one halo row above, columns x0-4 .. x0+tx+3
             self.oy = 1 if has_v else 0
+            self.ox = 4
+            self.rx = self.tx + 8
+        elif self.layout == 2:
+            # two-step region: two halo rows above, columns x0-4 .. x0+tx+3
+            self.oy = 2
             self.ox = 4
             self.rx = self.tx + 8
         else:
@@ -56,7 +67,10 @@ class TileGeometry:
         return tile, pos
 
     def placements(self, cell, role):
-        """(tile, pos, index into ``cell``) of every tile slot a flux cell occupies."""
+        """(tile, pos, index into ``cell``, primary) of every tile slot a cell
+        occupies; ``primary`` marks one placement per cell (the owning tile's slot)."""
+        if self.layout == 2:
+            return self._ring_placements(cell, role)
         tiles, poss = self.owner(cell)
         src = np.arange(cell.size)
         out_t, out_p, out_s = [tiles], [poss], [src]
@@ -89,7 +103,51 @@ class TileGeometry:
                 out_t.append(ty * self.tiles_x + tx)
                 out_p.append((self.ty + self.oy) * self.rx + (x[m] - tx * self.tx) + self.ox)
                 out_s.append(src[m])
-        return np.concatenate(out_t), np.concatenate(out_p), np.concatenate(out_s)
+        primary = np.zeros(sum(t.size for t in out_t), np.int32)
+        primary[:cell.size] = 1
+        return np.concatenate(out_t), np.concatenate(out_p), np.concatenate(out_s), primary
+
+    def _ring_placements(self, cell, role):
+        """Layout 2: every slot of every tile's first-step ring where ``cell`` is
+        computed. Slots are addressed by flat index, so a cell (x, y) also sits at
+        (x + k*nx, y - k) wherever that column lies in a tile's ring (row-end wrap;
+        several aliases per tile on grids narrower than the ring)."""
+        ml, mr, ma, mb = self.RING[role]
+        x0 = cell % self.nx
+        y0 = cell // self.nx
+        src0 = np.arange(cell.size)
+        kmin = -((self.tiles_x * self.tx + mr + self.nx) // self.nx) - 1
+        kmax = (ml + self.tiles_x * self.tx + self.nx) // self.nx + 1
+        own_t, own_p = self.owner(cell)
+        out_t, out_p, out_s, out_q = [], [], [], []
+        for k in range(kmin, kmax + 1):
+            X = x0 + k * self.nx
+            Y = y0 - k
+            # tiles whose ring [t*tx - ml, t*tx + tx - 1 + mr] contains X: at most
+            # ceil((ml + mr) / tx) + 1 consecutive tile columns (two for the kernel's
+            # tiles; more for tiles narrower than the margins)
+            for dtx in range((ml + mr + self.tx - 1) // self.tx + 1):
+                tx = (X + ml) // self.tx - dtx
+                okx = (tx >= 0) & (tx < self.tiles_x) & (X >= tx * self.tx - ml) & \
+                    (X <= tx * self.tx + self.tx - 1 + mr)
+                for dty in range((ma + mb + self.ty - 1) // self.ty + 1):
+                    ty = (Y + ma) // self.ty - dty
+                    ok = okx & (ty >= 0) & (ty < self.tiles_y) & (Y >= ty * self.ty - ma) & \
+                        (Y <= ty * self.ty + self.ty - 1 + mb)
+                    if not ok.any():
+                        continue
+                    t = ty[ok] * self.tiles_x + tx[ok]
+                    pos = (Y[ok] - ty[ok] * self.ty + self.oy) * self.rx + \
+                        (X[ok] - tx[ok] * self.tx) + self.ox
+                    out_t.append(t)
+                    out_p.append(pos)
+                    out_s.append(src0[ok])
+                    out_q.append(((t == own_t[ok]) & (pos == own_p[ok])).astype(np.int32))
+        if not out_t:
+            z = np.zeros(0, np.int64)
+            return z, z, z, np.zeros(0, np.int32)
+        return (np.concatenate(out_t), np.concatenate(out_p), np.concatenate(out_s),
+                np.concatenate(out_q))
 
 
 class SignalPool:
@@ -226,12 +284,13 @@ def compile_bounds(boundaries, n, pool, step_end, geo, role, offset=0.0):
     ops = ops[order]
     ucells, start = np.unique(cells, return_index=True)
     end = np.append(start[1:], cells.size)
-    tiles, pos, src = geo.placements(ucells, role)
+    tiles, pos, src, primary = geo.placements(ucells, role)
     o2 = np.lexsort((pos, tiles))  # by tile, then slot (row-major within the tile)
-    tiles, pos, src = tiles[o2], pos[o2], src[o2]
+    tiles, pos, src, primary = tiles[o2], pos[o2], src[o2], primary[o2]
     groups = np.zeros(tiles.size, dtype=_capi.BOUND_GROUP_DTYPE)
     groups["cell"] = ucells[src]
     groups["pos"] = pos
+    groups["primary"] = primary
     groups["op_begin"] = start[src]
     groups["op_end"] = end[src]
     tile_start = np.searchsorted(tiles, np.arange(geo.ntiles + 1)).astype(np.int32)

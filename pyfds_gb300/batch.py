@@ -39,7 +39,8 @@ class BatchRunner:
             if not f.matrices_assembled:
                 f.assemble_matrices()
         self.step0 = int(f0.step)
-        self.plans = [f._engine().prepare(self.step0, self.num_steps) for f in self.fields]
+        self.plans = [f._engine().prepare(self.step0, self.num_steps, batched=True)
+                      for f in self.fields]
         n = len(self.fields)
         self.probs = (_capi.FdsStagProblem * n)(*[p["prob"] for p in self.plans])
         self.tables = (_capi.FdsStagTables * n)(*[p["tstruct"] for p in self.plans])

@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(256) stag_batch_prologue_kernel(
     const int e = tb.bound_tile_start[a.ntiles];
     for (int g = threadIdx.x; g < e; g += blockDim.x) {
       const FdsBoundGroup grp = tb.groups[g];
+      if (!grp.primary) continue;  // the global array: once per cell
       TP v = p[grp.cell];
       for (int o = grp.op_begin; o < grp.op_end; ++o) {
         const FdsBoundOp op = tb.ops[o];

@@ -90,6 +90,7 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
   using namespace fds;
   if (!prob || !state || !tables) return set_error(FDS_E_ARG, "null argument");
   if (prob->nx < 1 || prob->ny < 1) return set_error(FDS_E_ARG, "bad grid %d x %d", prob->nx, prob->ny);
+  if (prob->stages < 0 || prob->stages > 3) return set_error(FDS_E_ARG, "bad stages %d", prob->stages);
   if (nsteps < 0 || step0 < 0) return set_error(FDS_E_ARG, "bad step range");
   const bool has_v = (prob->flags & FDS_FLAG_HAS_V) != 0;
   if (!has_v && prob->ny != 1) return set_error(FDS_E_ARG, "1-D field needs ny == 1");
@@ -163,6 +164,9 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
         p.tile_x != p0.tile_x || p.tile_y != p0.tile_y || p.stages != p0.stages)
       return set_error(FDS_E_ARG, "instance %d differs from instance 0 in variant or tile", i);
     if (p.nx < 1 || p.ny < 1) return set_error(FDS_E_ARG, "instance %d: bad grid", i);
+    if (p.stages < 0 || p.stages > 2)
+      return set_error(FDS_E_ARG, "instance %d: batched runs take stages 0, 1 or 2 (two steps "
+                       "per tile run single fields)", i);
     if (!(p.flags & FDS_FLAG_HAS_V) || (p.flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT | FDS_FLAG_FLOW)))
       return set_error(FDS_E_NOKERNEL, "batched runs cover lossless 2-D non-exact fields");
     if (!p.coefs.bx || !p.coefs.kx) return set_error(FDS_E_ARG, "instance %d: missing coefficients", i);

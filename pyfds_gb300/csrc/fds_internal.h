@@ -15,6 +15,8 @@
 #define FDS_TILE_MENU(X)                                                                   \
   X(64, 16, 256) X(32, 32, 256) X(128, 8, 256) X(64, 32, 512) X(128, 16, 512) X(64, 12, 256) \
   X(64, 8, 256)
+// two steps per tile (stages = 3): shared-memory tiles of slot layout 2
+#define FDS_TB2_MENU(X) X(64, 16, 256) X(64, 12, 256) X(64, 8, 256) X(32, 32, 256)
 #define FDS_MARCH_MENU(X) X(2, 16, 4) X(2, 8, 4) X(2, 32, 4) X(1, 16, 4) X(1, 32, 4)
 
 namespace fds {

@@ -61,6 +61,7 @@ __device__ void apply_bounds(const FdsCompTables& tb, int t, double* x, const do
   const int e = tb.bound_tile_start[t + 1];
   for (int g = tb.bound_tile_start[t] + threadIdx.x; g < e; g += blockDim.x) {
     const FdsBoundGroup grp = tb.groups[g];
+    if (!grp.primary) continue;  // the global array: once per cell (not halo copies)
     double val = x[grp.cell];
     for (int o = grp.op_begin; o < grp.op_end; ++o) {
       const FdsBoundOp op = tb.ops[o];

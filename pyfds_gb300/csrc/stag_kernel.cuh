@@ -80,6 +80,7 @@ struct StagCore {
   int32_t ntiles;
   int32_t use_tma;  // stage the region with TMA boxes (tm[]) instead of cp.async
   int32_t prefetch; // TMA path: also prefetch into L2 the region of tile + prefetch (0: off)
+  int32_t substeps; // two-step kernel: steps this launch advances (1 or 2)
   int32_t* status;  // OR-ed with kStatus* bits; may be null
   double offset;    // potential stored as value - offset (thermal float32), else 0
 };
@@ -744,6 +745,120 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
   }
 }
 
+// ------------------------------------------------------------ two steps per tile
+//
+// Temporal blocking for the lossless 2-D variants (memory-bound precisions): a
+// CTA stages a region two rows taller than the one-step kernel's (rows y0-2 ..
+// y0+TY+1, columns x0-4 .. x0+TX+3; slot layout 2), computes step n on a ring one
+// cell wider than the tile (fluxes on U: x0-1 .. x0+TX+1 x y0-1 .. y0+TY, V: x0-1
+// .. x0+TX x y0-1 .. y0+TY+1, potential on x0-1 .. x0+TX x y0-1 .. y0+TY), then
+// step n+1 on the tile exactly as the one-step kernel does, and stores the owned
+// cells once: the state crosses HBM once per two steps. Every cell is computed in
+// the one-step kernel's operation order, so the results are the same bit for bit.
+// The bound tables of layout 2 hold every slot of the ring where a bound cell is
+// computed; applying step n+1's bounds to ring slots that step n+1 does not
+// recompute is harmless (they are neither read nor stored). Probes belong to the
+// owning tile only.
+template <int TX_, int TY_, int NT_, bool MEMORY_>
+struct Tb2Cfg : StagCfg<TX_, TY_, NT_, true, MEMORY_, false, false, false, 1> {
+  static constexpr int OY = 2;
+  static constexpr int RY = TY_ + 4;
+  static constexpr int RN = (TX_ + 8) * RY;
+};
+
+// New potential at slot ps (lossless, float64 / float32 / double words): the
+// one-stage kernel's expression, term by term.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TP potential_new(const StagBuf<TP, TF, TC>& b, int ps) {
+  TF acc = (TF)b.P[ps];
+  acc = fma((TF)b.Kx[ps], b.U[ps], acc);
+  acc = fma(-(TF)b.Kx[ps + 1], b.U[ps + 1], acc);
+  acc = fma((TF)b.Ky[ps], b.V[ps], acc);
+  acc = fma(-(TF)b.Ky[ps + C::RX], b.V[ps + C::RX], acc);
+  return (TP)settle(acc);
+}
+
+// Step si.step on the ring around the tile, in place in the staged region.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void compute_ring(const StagCore<TP, TF, TC>& a, const StepInfo si,
+                                             int tile, const StagBuf<TP, TF, TC>& b) {
+  constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, OX = C::OX, OY = C::OY;
+  const int x0 = (tile % a.tiles_x) * TX;
+  const int y0 = (tile / a.tiles_x) * TY;
+  // fluxes: each slot reads only its own old flux and the potential. Slots of
+  // cells outside the field get 0, as in the one-step kernel (thermal fluxes are
+  // not staged, so those slots would otherwise hold stale shared memory, which the
+  // potential update multiplies by a zero coefficient)
+  constexpr int UW = TX + 3, UH = TY + 2, VW = TX + 2, VH = TY + 3;
+  for (int c = threadIdx.x; c < UW * UH; c += NT) {
+    const int lx = c % UW - 1, ly = c / UW - 1;
+    const int pos = (ly + OY) * RX + lx + OX;
+    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
+    b.U[pos] = (f >= 0 && f < a.n) ? flux_new<C, true>(a, b.P, b.U, b.Bx, pos, f, 0) : TF(0);
+  }
+  for (int c = threadIdx.x; c < VW * VH; c += NT) {
+    const int lx = c % VW - 1, ly = c / VW - 1;
+    const int pos = (ly + OY) * RX + lx + OX;
+    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
+    b.V[pos] = (f >= 0 && f < a.n) ? flux_new<C, false>(a, b.P, b.V, b.By, pos, f, 0) : TF(0);
+  }
+  __syncthreads();
+  apply_bound_groups<NT>(a.tab[1], tile, b.U, a.pool, si.step);
+  apply_bound_groups<NT>(a.tab[2], tile, b.V, a.pool, si.step);
+  __syncthreads();
+  write_probes<NT>(a.tab[1], tile, b.U, si.step - si.step0);
+  write_probes<NT>(a.tab[2], tile, b.V, si.step - si.step0);
+  // potential of step si.step + 1: each slot reads only its own old value
+  constexpr int PW = TX + 2, PH = TY + 2;
+  for (int c = threadIdx.x; c < PW * PH; c += NT) {
+    const int lx = c % PW - 1, ly = c / PW - 1;
+    const int pos = (ly + OY) * RX + lx + OX;
+    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
+    if (f >= 0 && f < a.n) b.P[pos] = potential_new<C>(b, pos);
+  }
+  __syncthreads();
+  apply_bound_groups<NT>(a.tab[0], tile, b.P, a.pool, si.step + 1);
+  __syncthreads();
+  write_probes<NT>(a.tab[0], tile, b.P, si.step + 1 - si.step0);
+}
+
+// One tile, one or two steps (a.substeps), one CTA per tile, TMA or cp.async
+// staging, L2 prefetch of a later tile as in the one-step kernel.
+template <class C, typename TP, typename TF, typename TC>
+__global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<TP, dw>::value))
+    stag_tb2_kernel(const __grid_constant__ StagArgs<TP, TF, TC> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const bool iso = a.iso != 0;
+  const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(iso);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + bytes);
+  const bool tma = a.use_tma && (smem_addr(smem_raw) & 127u) == 0;
+  const StagBuf<TP, TF, TC> buf = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
+  const int t = blockIdx.x;
+  if (tma && threadIdx.x == 0) mbar_init(bars, 1);
+  __syncthreads();
+  if (tma) {
+    if (threadIdx.x == 0) {
+      tma_issue_tile<C>(a, a.tm, t, buf, iso, bars);
+      if (a.prefetch > 0 && t + a.prefetch < a.ntiles)
+        tma_prefetch_tile<C>(a, a.tm, t + a.prefetch, iso);
+    }
+    if (!tma_finish_tile<C>(a, t, buf, iso, bars, 0)) return;
+  } else {
+    stage_tile<C>(a, t, buf, iso);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+  }
+  const StepInfo si = step_of(a);
+  if (a.substeps == 2) {
+    compute_ring<C>(a, si, t, buf);
+    __syncthreads();
+    compute_tile<C>(a, StepInfo{si.step + 1, si.step0, si.apply_next, si.store_flux}, t, buf);
+  } else {
+    compute_tile<C>(a, si, t, buf);
+  }
+}
+
 // Potential bounds and probes of the first step of a call, in place on the
 // global potential (one CTA: bounds, barrier, probes).
 template <typename TP>
@@ -754,6 +869,7 @@ __global__ void __launch_bounds__(1024) stag_prologue_kernel(TP* p, FdsCompTable
     const int e = tb.bound_tile_start[ntiles];
     for (int g = threadIdx.x; g < e; g += blockDim.x) {
       const FdsBoundGroup grp = tb.groups[g];
+      if (!grp.primary) continue;  // the global array: once per cell (not halo copies)
       TP v = p[grp.cell];
       for (int o = grp.op_begin; o < grp.op_end; ++o) {
         const FdsBoundOp op = tb.ops[o];

@@ -116,6 +116,41 @@ int32_t launch_stag(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
   return FDS_OK;
 }
 
+// Launch one or two steps (a.substeps) of the two-step kernel: one CTA per tile.
+template <class C, typename TP, typename TF, typename TC>
+int32_t launch_tb2(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
+  const bool iso = a.iso != 0;
+  const size_t smem = stag_buffer_bytes<C, TP, TF, TC>(iso) + 16;
+  static int optin = -1, nsm = -1;
+  static size_t attr_bytes = 0;
+  static int occ[2] = {-1, -1};
+  if (optin < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  if (smem > (size_t)optin)
+    return set_error(FDS_E_SIZE, "two-step tile %dx%d needs %zu bytes of shared memory "
+                     "(device allows %d)", C::TX, C::TY, smem, optin);
+  if (smem > attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(stag_tb2_kernel<C, TP, TF, TC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
+    attr_bytes = smem;
+  }
+  select_tma<C>(a, tc, tc ? tc->state : nullptr);
+  int& o = occ[iso ? 1 : 0];
+  if (o < 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &o, stag_tb2_kernel<C, TP, TF, TC>, C::NT, smem);
+    if (e != cudaSuccess || o < 1) o = 1;
+  }
+  a.prefetch = a.use_tma ? (int32_t)(0.4 * o * nsm) : 0;
+  stag_tb2_kernel<C, TP, TF, TC><<<a.ntiles, C::NT, smem, s>>>(a);
+  return FDS_OK;
+}
+
 template <class C, typename TP, typename TF, typename TC>
 int32_t launch_march(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache*) {
   const int grid = (a.ntiles + C::NW - 1) / C::NW;
@@ -132,6 +167,23 @@ StagLaunch<TP, TF, TC> pick_stag(int family, bool has_v, bool absorb, bool axi, 
   if (exact && !ALLOW_EXACT) return nullptr;
   if (acoustic && !ALLOW_ACOUSTIC) return nullptr;
   if (!acoustic && absorb) return nullptr;
+  if (stages == 3) {
+    // two steps per tile: lossless 2-D (axisymmetric without losses steps as planar),
+    // potential and fluxes of one type
+    if constexpr (sizeof(TP) == sizeof(TF)) {
+#define FDS_PICK_TB2(TX, TY, NT)                                                            \
+  if (has_v && !absorb && !exact && tx == TX && ty == TY) {                                  \
+    if (acoustic) {                                                                         \
+      if constexpr (ALLOW_ACOUSTIC) return &launch_tb2<Tb2Cfg<TX, TY, NT, true>, TP, TF, TC>; \
+    } else {                                                                                \
+      return &launch_tb2<Tb2Cfg<TX, TY, NT, false>, TP, TF, TC>;                            \
+    }                                                                                       \
+  }
+      FDS_TB2_MENU(FDS_PICK_TB2)
+#undef FDS_PICK_TB2
+    }
+    return nullptr;
+  }
   // the radius only enters the kernel through the exact pressure scaling and the
   // radial loss term; otherwise the axisymmetric step is the planar one
   if (axi && !exact && !absorb) axi = false;
@@ -205,10 +257,16 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   // stages: 0 (automatic) and 1 = one CTA per tile; 2 = the persistent two-stage
   // pipeline (built for the tile menu; measured slower on GB300 for one field)
   StagLaunch<TP, TF, TC> fn = nullptr;
-  if (prob->stages == 2)
+  const bool two_step = prob->stages == 3;
+  if (two_step) {
+    if (flow) return set_error(FDS_E_ARG, "two steps per tile do not cover a moving medium");
+    fn = pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi,
+                                                            exact, prob->tile_x, prob->tile_y, 3);
+  } else if (prob->stages == 2)
     fn = pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi,
                                                             exact, prob->tile_x, prob->tile_y, 2);
-  if (!fn && prob->stages != 2)
+  // a two-step request never falls back: its tables are built for slot layout 2
+  if (!fn && prob->stages != 2 && !two_step)
     fn = pick_stag<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, has_v, absorb, axi,
                                                             exact, prob->tile_x, prob->tile_y, 1);
   if (!fn)
@@ -262,7 +320,10 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
   }
-  for (int32_t s = 0; s < nsteps; ++s) {
+  for (int32_t s = 0; s < nsteps;) {
+    // the two-step kernel advances two steps per launch (one for an odd last step)
+    const int take = (two_step && s + 1 < nsteps) ? 2 : 1;
+    a.substeps = take;
     a.p_in = (const TP*)st->cur[0];
     a.p_out = (TP*)st->nxt[0];
     a.u_in = (const TF*)st->cur[1];
@@ -272,8 +333,8 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
     a.step = step0 + s;
     // a moving medium shifts rows between the pressure update and the next step's
     // pressure bounds / probes, which then run in the prologue kernel instead
-    a.apply_next = (s + 1 < nsteps && !flow) ? 1 : 0;
-    a.store_flux = (store_flux || s + 1 == nsteps) ? 1 : 0;
+    a.apply_next = (s + take < nsteps && !flow) ? 1 : 0;
+    a.store_flux = (store_flux || s + take == nsteps) ? 1 : 0;
     const int32_t rc = fn(a, stream, &tma);
     if (rc != FDS_OK) return rc;
     cudaError_t e = cudaGetLastError();
@@ -290,6 +351,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
           return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
       }
     }
+    s += take;
   }
   return FDS_OK;
 }

@@ -26,7 +26,7 @@ class _NlEngine(StagEngine):
         512 tiles so that every CTA stays resident."""
         return 64 * max(1, -(-n // (64 * 512)))
 
-    def _geometry(self):
+    def _geometry(self, batched=False):
         n = self.field.num_points
         return _tables.TileGeometry(n, 1, self.tile_cells(n), 1, False, 0)
 

@@ -140,3 +140,60 @@ def test_table_slots_decode_to_their_cells(layout, tile, nx, ny):
     for t in range(geo.ntiles):
         for q in pt["probes"][ts[t]:ts[t + 1]]:
             assert _decode(geo, t, q["pos"]) == q["cell"]
+
+
+@pytest.mark.parametrize("nx,ny,tx,ty", [(37, 19, 8, 4), (5, 9, 8, 4), (1, 7, 8, 4), (64, 24, 16, 8),
+                                         (3, 1, 8, 4), (17, 2, 4, 4), (9, 7, 1, 1), (7, 5, 2, 1),
+                                         (6, 6, 3, 2)])
+def test_two_step_ring_placements_match_brute_force(nx, ny, tx, ty):
+    """Layout 2 (two steps per tile): a cell's bound group is placed at exactly the
+    slots of each tile's first-step ring whose flat index is that cell, for every
+    component's ring, including row-end wrap aliases and grids narrower than a tile."""
+    from pyfds_gb300 import _tables as T
+    geo = T.TileGeometry(nx, ny, tx, ty, True, layout=2)
+    n = nx * ny
+    cells = np.arange(n)
+    for role, (ml, mr, ma, mb) in T.TileGeometry.RING.items():
+        want = set()
+        for t in range(geo.ntiles):
+            x0 = (t % geo.tiles_x) * tx
+            y0 = (t // geo.tiles_x) * ty
+            for Y in range(y0 - ma, y0 + ty + mb):
+                for X in range(x0 - ml, x0 + tx + mr):
+                    f = Y * nx + X
+                    if 0 <= f < n:
+                        pos = (Y - y0 + geo.oy) * geo.rx + (X - x0) + geo.ox
+                        want.add((t, pos, f))
+        tiles, pos, src, primary = geo.placements(cells, role)
+        got = set(zip(tiles.tolist(), pos.tolist(), cells[src].tolist()))
+        assert got == want, (role, len(got), len(want))
+        assert len(got) == tiles.size  # no duplicates
+        # one primary placement per cell: its owner's slot
+        assert np.array_equal(np.sort(src[primary == 1]), cells)
+        own_t, own_p = geo.owner(cells[src[primary == 1]])
+        assert np.array_equal(own_t, tiles[primary == 1])
+        assert np.array_equal(own_p, pos[primary == 1])
+
+
+TWO_STEP_CASES = []
+for seed in range(40, 64):
+    kind = ["Acoustic2D", "Thermal2D", "Acoustic3DAxi", "Thermal3DAxi"][seed % 4]
+    TWO_STEP_CASES.append((seed, kind, [9, 7, 5, 11, 8, 3, 1][seed % 7],
+                           [7, 6, 9, 4, 5, 2][(seed // 7) % 6],
+                           [(4, 3), (3, 2), (2, 2), (8, 4), (1, 1), (4, 4)][seed % 6],
+                           [6, 7, 1, 2][seed % 4]))
+
+
+@pytest.mark.parametrize("seed,kind,nx,ny,tile,steps", TWO_STEP_CASES)
+def test_two_step_kernel_model_matches_oracle(seed, kind, nx, ny, tile, steps):
+    """Two steps per tile (layout-2 tables, the first step on a ring around the
+    tile): bit for bit the oracle, for odd and even step counts, on tiny tiles and
+    grids narrower than a tile, every boundary and output mode."""
+    spec = S.random_scenario(seed, kind, nx, ny, steps=steps, mu=False)
+    st_o, sg_o = O.simulate(spec, spec["steps"])
+    f = build_field(spec, exact=True)
+    st_m, sg_m = KernelModel(f, tile=tile, two_step=True).run(spec["steps"])
+    for c in st_o:
+        assert np.array_equal(st_o[c], st_m[c]), c
+        for a, b in zip(sg_o[c], sg_m[c]):
+            assert np.array_equal(a, b), c
