@@ -239,11 +239,12 @@ def run_batched(args):
     cells = sum(f.num_points for f in fields)
     tile = tuple(int(v) for v in args.tile.split("x")) if args.tile else \
         ((64, 12) if args.precision == "dw" else (64, 16))
-    stages = args.stages or 1
+    stages = args.stages or None  # None: the engine's choice (two steps per tile)
     if args.autotune:
         from pyfds_gb300.autotune import autotune_batch
         tile, stages = autotune_batch(fields, steps=20)
     runner = BatchRunner(fields, nt, tile=tile, stages=stages)
+    stages = int(runner.probs[0].stages)
     runner.capture()
 
     def reset():
@@ -277,7 +278,9 @@ def run_batched(args):
     barrier()
     ms = _max_over_ranks(total_ms / args.steps)
     value = ws * cells * nt / (ms * 1e-3) / 1e9
-    launch_ms = ms / nt
+    spl = runner.steps_per_launch()
+    step_ms = ms / nt
+    launch_ms = step_ms * spl
     # e2e: the public API with host state and host outputs, every step
     e2e_steps = 0 if args.no_e2e else 1
     h2d = d2h = 0
@@ -306,7 +309,7 @@ def run_batched(args):
         return 0
     peak, peak_kind = _peaks()
     bpc = balg.get(args.precision)
-    achieved = cells * bpc / (launch_ms * 1e-3) / 1e9 if bpc else None
+    achieved = cells * bpc / (step_ms * 1e-3) / 1e9 if bpc else None
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -326,11 +329,13 @@ def run_batched(args):
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None,
-                         "traffic": _traffic_from_profiles("batched_%s" % args.precision),
+                         "traffic": _traffic_from_profiles(
+                             "batched_%s%s" % (args.precision, "_tb2" if spl == 2 else "")),
                          "peak_kind": peak_kind, "kernel": "stag_batch_kernel",
-                         "bytes_per_cell": bpc, "launch_ms": launch_ms},
+                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl},
             "clocks": clk.summary(),
-            "gpu_launches": int(args.steps * (nt + 1))}
+            # per replay: the prologue, then one launch per step (per two with stages 3)
+            "gpu_launches": int(args.steps * (runner.launches() + 1))}
     if ws == 1 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         steps = CPU_SAMPLE_STEPS["batched"]

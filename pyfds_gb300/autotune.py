@@ -1,4 +1,5 @@
-"""Autotuner for the batched step: tile shape and pipeline depth per size class.
+"""Autotuner for the batched step: tile shape, pipeline depth and temporal blocking
+(one or two steps per tile and launch) per size class.
 
 Candidates are timed on the real batch for a few steps (CUDA events on the
 launching stream, warm-up first); the winner is cached in a JSON file keyed by
@@ -12,8 +13,11 @@ import os
 from . import _capi
 from ._engine import require_cuda
 
+# (tile, stages): one step per tile and launch (1), the persistent two-stage pipeline
+# (2), two steps per tile and launch (3: temporal blocking)
 CANDIDATES = [((64, 16), 1), ((32, 32), 1), ((128, 8), 1), ((64, 32), 1), ((128, 16), 1),
-              ((64, 16), 2), ((32, 32), 2), ((128, 8), 2)]
+              ((64, 16), 2), ((32, 32), 2), ((128, 8), 2),
+              ((64, 16), 3), ((64, 12), 3), ((32, 32), 3), ((64, 8), 3)]
 
 
 def cache_path():
@@ -59,7 +63,8 @@ def autotune_batch(fields, steps=20, candidates=CANDIDATES, force=False, verbose
     if key in cache and not force:
         tile, stages = tuple(cache[key]["tile"]), int(cache[key]["stages"])
     else:
-        steps += steps % 2  # even: the ping-pong buffers end where they started
+        steps += (-steps) % 4  # even launches for one or two steps per launch: the
+        # ping-pong buffers end where they started
         saved_tile = [getattr(f, "tile", None) for f in fields]
         first = BatchRunner(fields, steps)  # uploads the host state
         snapshot = [{n: b[0].clone() for n, b in f._engine().buffers.items()} for f in fields]

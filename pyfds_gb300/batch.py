@@ -79,13 +79,24 @@ class BatchRunner:
         self._fill_states()
         self._call(_capi.BATCH_LAUNCH)
 
+    def steps_per_launch(self):
+        """2 when the batch runs two steps per tile (stages 3), else 1."""
+        return 2 if int(self.probs[0].stages) == 3 else 1
+
+    def launches(self):
+        """Kernel launches of one run (launch_count)."""
+        return launch_count(self.num_steps, self.steps_per_launch())
+
     def capture(self, warmup=True):
-        """Capture ``launch`` in a CUDA graph (an even step count keeps the ping-pong
-        buffers of every replay in the same place). The warm-up launch before the
-        capture (kernel attributes, caches) advances the fields; ``warmup=False``
-        skips it, for a process that has already launched this kernel variant."""
-        if self.num_steps % 2:
-            raise ValueError("graph replays need an even number of steps")
+        """Capture ``launch`` in a CUDA graph (an even number of kernel launches keeps
+        the ping-pong buffers of every replay in the same place: an even step count,
+        or any count of two or more with two steps per tile). The warm-up launch
+        before the capture (kernel attributes, caches) advances the fields;
+        ``warmup=False`` skips it, for a process that has already launched this
+        kernel variant."""
+        if self.launches() % 2:
+            raise ValueError("graph replays need an even number of launches (%d steps, %d "
+                             "launches)" % (self.num_steps, self.launches()))
         torch = self.torch
         if warmup:
             self.launch()
@@ -108,6 +119,19 @@ class BatchRunner:
             eng._last = plan
             eng.finish(plan)
             f.step += self.num_steps
+
+
+def launch_count(num_steps, steps_per_launch):
+    """Kernel launches fds_stag_batch_run issues for a run: one per step, or with two
+    steps per tile n2 launches of two steps, then n1 of one, with n2 + n1 even
+    whenever there are two steps or more."""
+    n = int(num_steps)
+    if steps_per_launch == 1:
+        return n
+    n2, n1 = n // 2, n % 2
+    if (n2 + n1) % 2 and n2 > 0:
+        n2, n1 = n2 - 1, n1 + 2
+    return n2 + n1
 
 
 def simulate_batch(fields, num_steps=None, tile=None, stages=None):

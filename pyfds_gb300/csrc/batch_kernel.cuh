@@ -5,7 +5,8 @@
 // ping-pong parity: parity 0 reads `cur` and writes `nxt`, parity 1 the reverse),
 // holding its grid, coefficient pointers, tables and the TMA tensor maps of the
 // arrays it reads. A work list of (instance, tile) pairs covers every tile of
-// every instance. STAGES == 1: one CTA per work item, which also prefetches into
+// every instance (a two-step configuration advances it two steps when the launch's
+// StepInfo says so). STAGES == 1: one CTA per work item, which also prefetches into
 // L2 the region of the item `prefetch` places ahead. STAGES == 2: persistent
 // CTAs walk the work list, prefetching the next item's region (possibly another
 // instance's) while computing the current one.
@@ -72,6 +73,15 @@ __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
       cp_async_commit();
       cp_async_wait<0>();
       __syncthreads();
+    }
+    if constexpr (C::TWO_STEP) {
+      if (si.substeps == 2) {  // steps si.step and si.step + 1 of this tile
+        compute_ring<C>(a, si, it.y, buf);
+        __syncthreads();
+        compute_tile<C>(a, StepInfo{si.step + 1, si.step0, si.apply_next, si.store_flux, 1},
+                        it.y, buf);
+        return;
+      }
     }
     compute_tile<C>(a, si, it.y, buf);
   } else {

@@ -164,9 +164,7 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
         p.tile_x != p0.tile_x || p.tile_y != p0.tile_y || p.stages != p0.stages)
       return set_error(FDS_E_ARG, "instance %d differs from instance 0 in variant or tile", i);
     if (p.nx < 1 || p.ny < 1) return set_error(FDS_E_ARG, "instance %d: bad grid", i);
-    if (p.stages < 0 || p.stages > 2)
-      return set_error(FDS_E_ARG, "instance %d: batched runs take stages 0, 1 or 2 (two steps "
-                       "per tile run single fields)", i);
+    if (p.stages < 0 || p.stages > 3) return set_error(FDS_E_ARG, "instance %d: bad stages", i);
     if (!(p.flags & FDS_FLAG_HAS_V) || (p.flags & (FDS_FLAG_ABSORB | FDS_FLAG_EXACT | FDS_FLAG_FLOW)))
       return set_error(FDS_E_NOKERNEL, "batched runs cover lossless 2-D non-exact fields");
     if (!p.coefs.bx || !p.coefs.kx) return set_error(FDS_E_ARG, "instance %d: missing coefficients", i);

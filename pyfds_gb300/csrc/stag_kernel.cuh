@@ -97,11 +97,12 @@ struct StepInfo {
   int64_t step0;
   int32_t apply_next;
   int32_t store_flux;
+  int32_t substeps;  // two-step kernels: steps of this launch (1 or 2)
 };
 
 template <typename TP, typename TF, typename TC>
 __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
-  return StepInfo{a.step, a.step0, a.apply_next, a.store_flux};
+  return StepInfo{a.step, a.step0, a.apply_next, a.store_flux, a.substeps};
 }
 
 // Resident CTAs per SM the 256-thread 2-D tile kernels are compiled for (the
@@ -126,6 +127,7 @@ __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
           bool EXACT_, int STAGES_ = 1>
 struct StagCfg {
+  static constexpr bool TWO_STEP = false;  // two steps per tile (Tb2Cfg)
   static constexpr int STAGES = STAGES_;  // staging buffers (2: persistent, prefetching)
   static constexpr int TX = TX_;
   static constexpr int TY = TY_;
@@ -761,6 +763,7 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
 // owning tile only.
 template <int TX_, int TY_, int NT_, bool MEMORY_>
 struct Tb2Cfg : StagCfg<TX_, TY_, NT_, true, MEMORY_, false, false, false, 1> {
+  static constexpr bool TWO_STEP = true;
   static constexpr int OY = 2;
   static constexpr int RY = TY_ + 4;
   static constexpr int RN = (TX_ + 8) * RY;
@@ -853,7 +856,7 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
   if (a.substeps == 2) {
     compute_ring<C>(a, si, t, buf);
     __syncthreads();
-    compute_tile<C>(a, StepInfo{si.step + 1, si.step0, si.apply_next, si.store_flux}, t, buf);
+    compute_tile<C>(a, StepInfo{si.step + 1, si.step0, si.apply_next, si.store_flux, 1}, t, buf);
   } else {
     compute_tile<C>(a, si, t, buf);
   }

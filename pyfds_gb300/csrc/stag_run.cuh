@@ -474,15 +474,27 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch prologue: %s", cudaGetErrorString(e));
   }
-  for (int32_t s = 0; s < nsteps; ++s) {
-    const StepInfo si{step0 + s, step0, (s + 1 < nsteps) ? 1 : 0,
-                      (store_flux || s + 1 == nsteps) ? 1 : 0};
+  // one step per launch, or for a two-step configuration n2 launches of two steps
+  // then n1 of one, with n2 + n1 even whenever nsteps >= 2 (a captured run then ends
+  // with the ping-pong buffers where it started); the parity follows the launches
+  int32_t n2 = C::TWO_STEP ? nsteps / 2 : 0;
+  int32_t n1 = nsteps - 2 * n2;
+  if (((n2 + n1) & 1) && n2 > 0) {
+    --n2;
+    n1 += 2;
+  }
+  int32_t launches = 0;
+  for (int32_t s = 0; s < nsteps; ++launches) {
+    const int take = launches < n2 ? 2 : 1;
+    const StepInfo si{step0 + s, step0, (s + take < nsteps) ? 1 : 0,
+                      (store_flux || s + take == nsteps) ? 1 : 0, take};
     stag_batch_kernel<C, TP, TF, TC><<<grid, C::NT, smem, stream>>>(d_desc, d_work, (int)nwork, si,
-                                                                    s & 1, prefetch);
+                                                                    launches & 1, prefetch);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch step: %s", cudaGetErrorString(e));
+    s += take;
   }
-  if (nsteps & 1)
+  if (launches & 1)
     for (int i = 0; i < count; ++i)
       for (int k = 0; k < 3; ++k) std::swap(states[i].cur[k], states[i].nxt[k]);
   return FDS_OK;
@@ -496,6 +508,28 @@ int32_t run_batch_typed(const FdsStagProblem* probs, FdsStagState* states,
   const FdsStagProblem& p0 = probs[0];
   const bool acoustic = p0.family == FDS_FAMILY_ACOUSTIC;
   const int stages = p0.stages == 2 ? 2 : 1;
+  if (p0.stages == 3) {
+    // two steps per tile: potential and fluxes of one type
+    if constexpr (sizeof(TP) == sizeof(TF)) {
+#define FDS_BATCH_TB2(TX, TY, NT)                                                                \
+  if (p0.tile_x == TX && p0.tile_y == TY) {                                                      \
+    if (acoustic) {                                                                              \
+      if constexpr (ALLOW_ACOUSTIC)                                                              \
+        return batch_run_variant<Tb2Cfg<TX, TY, NT, true>, TP, TF, TC>(                          \
+            probs, states, tables, count, workspace, workspace_bytes, step0, nsteps, store_flux, \
+            mode, stream);                                                                       \
+    } else {                                                                                     \
+      return batch_run_variant<Tb2Cfg<TX, TY, NT, false>, TP, TF, TC>(                           \
+          probs, states, tables, count, workspace, workspace_bytes, step0, nsteps, store_flux,   \
+          mode, stream);                                                                         \
+    }                                                                                            \
+  }
+      FDS_TB2_MENU(FDS_BATCH_TB2)
+#undef FDS_BATCH_TB2
+    }
+    return set_error(FDS_E_NOKERNEL, "no two-step batched kernel for family=%d tile=%dx%d",
+                     p0.family, p0.tile_x, p0.tile_y);
+  }
 #define FDS_BATCH_TILE(TX, TY, NT)                                                              \
   if (p0.tile_x == TX && p0.tile_y == TY) {                                                     \
     if (acoustic) {                                                                             \

@@ -83,3 +83,45 @@ def test_two_step_rejects_what_it_does_not_cover(gpu):
     f.stages = 3
     with pytest.raises(_capi.FdsError):
         f.simulate(4)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "dw"])
+@pytest.mark.parametrize("kind", ["Acoustic2D", "Thermal2D"])
+def test_batched_two_step_equals_single_one_step(gpu, precision, kind):
+    """Six fields of uneven size batched with two steps per tile (odd step count):
+    each equals its single-field one-step run bit for bit."""
+    from pyfds_gb300.batch import simulate_batch
+    sizes = [(204, 77), (203, 64), (64, 256), (37, 19), (130, 130), (256, 32)]
+    specs = [S.random_scenario(90 + k, kind, nx, ny, steps=13, mu=False)
+             for k, (nx, ny) in enumerate(sizes)]
+    batch = [build_field(s, precision=precision) for s in specs]
+    simulate_batch(batch, 13, tile=(64, 16), stages=3)
+    for s, fb in zip(specs, batch):
+        assert_same(field_results(fb), run(s, precision, (64, 16), 1, 13))
+
+
+def test_batched_two_step_graph_replay(gpu):
+    """A captured two-step batch (8 steps = 4 launches) replays to the state of the
+    same launches issued directly."""
+    import torch
+    from pyfds_gb300.batch import BatchRunner
+    specs = [S.random_scenario(95 + k, "Acoustic2D", 96, 40 + 8 * k, steps=8, mu=False)
+             for k in range(3)]
+    a = [build_field(s, precision="f32") for s in specs]
+    b = [build_field(s, precision="f32") for s in specs]
+    ra = BatchRunner(a, 8, tile=(64, 16), stages=3)
+    assert ra.steps_per_launch() == 2
+    ra.capture()
+    ra.replay()
+    rb = BatchRunner(b, 8, tile=(64, 16), stages=3)
+    rb.launch()
+    rb.launch()
+    torch.cuda.synchronize()
+    for fa, fb in zip(a, b):
+        for name in fa._stag_components:
+            assert torch.equal(fa._engine().buffers[name][0], fb._engine().buffers[name][0]), name
+    # any step count of two or more captures: 6 steps run as 2 + 2 + 1 + 1
+    r6 = BatchRunner(b, 6, tile=(64, 16), stages=3)
+    assert r6.launches() == 4
+    with pytest.raises(ValueError):
+        BatchRunner(b, 1, tile=(64, 16), stages=3).capture()  # one launch

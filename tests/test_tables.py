@@ -197,3 +197,15 @@ def test_two_step_kernel_model_matches_oracle(seed, kind, nx, ny, tile, steps):
         assert np.array_equal(st_o[c], st_m[c]), c
         for a, b in zip(sg_o[c], sg_m[c]):
             assert np.array_equal(a, b), c
+
+
+def test_batched_launch_count():
+    """Launches of a batched run (mirrors the loop of fds_stag_batch_run): with two
+    steps per tile the count is even for every step count of two or more, so a
+    captured graph ends with the ping-pong buffers where it started."""
+    from pyfds_gb300.batch import launch_count
+    assert [launch_count(n, 1) for n in range(6)] == [0, 1, 2, 3, 4, 5]
+    assert [launch_count(n, 2) for n in range(1, 9)] == [1, 2, 2, 2, 4, 4, 4, 4]
+    for n in range(2, 200):
+        k = launch_count(n, 2)
+        assert k % 2 == 0 and n / 2 <= k <= n / 2 + 2
