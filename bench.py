@@ -782,7 +782,9 @@ def run_ours(args):
                       for n in field._stag_components)
     out_bytes = sum(o.numel() * 8 for o in last["outs"] if o is not None)
     h2d = state_bytes + coef_bytes + tab_bytes
-    d2h = out_bytes + result.size * eng.buffers[field._stag_components[0]][0].element_size()
+    # the final potential comes back as float64 for double words (joined on the device)
+    d2h = out_bytes + result.size * (8 if args.precision == "dw" else
+                                     eng.buffers[field._stag_components[0]][0].element_size())
     e2e_value = ws * cells * nt / e2e_s / 1e9 if e2e_steps else None
     if rank != 0:
         return 0

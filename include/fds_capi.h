@@ -304,6 +304,14 @@ int32_t fds_thermoacoustic_run(const FdsStagProblem* acoustic, FdsStagState* ac_
 int32_t fds_stag_flow_shift(const FdsStagProblem* prob, FdsStagState* state, int64_t step,
                             void* stream);
 
+/* Double words (FDS_PREC_DW) on the device: fds_dw_split turns n float64 values
+ * into {float hi, float lo} pairs (hi = (float)x, lo = (float)(x - hi), both rounded
+ * to nearest), fds_dw_join adds pairs back into float64 ((double)hi + (double)lo).
+ * Device pointers; `out` may not overlap `in`. (New: the host-side conversion of
+ * pyfds_gb300, done where the data already is.) */
+int32_t fds_dw_split(const double* in, void* out, int64_t n, void* stream);
+int32_t fds_dw_join(const void* in, double* out, int64_t n, void* stream);
+
 /* Workspace (device bytes, 256-byte aligned) a batched call over `count` instances
  * with `total_tiles` tiles in all needs: per-instance descriptors and the work
  * list. (New: no reference counterpart; the reference runs one field at a time.) */

@@ -50,7 +50,7 @@ BOP_SIGNAL = 2
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
                     "fds_stag_batch_run", "fds_stag_batch_run_static", "fds_stag_flow_shift",
-                    "fds_nl1d_run", "fds_thermoacoustic_run",
+                    "fds_nl1d_run", "fds_thermoacoustic_run", "fds_dw_split", "fds_dw_join",
                     # include/fds_surrogate.h
                     "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
                     "fds_conv_wgrad_max_grid", "fds_adamw", "fds_surr_pack", "fds_surr_loss",
@@ -210,18 +210,10 @@ def load(path=None):
     lib.fds_stag_flow_shift.restype = C.c_int32
     lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                         C.c_int64, C.c_void_p]
-    lib.fds_thermoacoustic_run.restype = C.c_int32
-    lib.fds_thermoacoustic_run.argtypes = [
-        C.POINTER(FdsStagProblem), C.POINTER(FdsStagState), C.POINTER(FdsStagTables),
-        C.POINTER(FdsStagProblem), C.POINTER(FdsStagState), C.POINTER(FdsStagTables),
-        C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32), C.c_double, C.c_int32,
-        C.c_int32, C.c_int64, C.c_int32, C.c_void_p]
-    lib.fds_nl1d_run.restype = C.c_int32
-    lib.fds_nl1d_run.argtypes = [C.POINTER(FdsNl1dProblem), C.POINTER(FdsStagState),
-                                 C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_void_p]
-    lib.fds_stag_flow_shift.restype = C.c_int32
-    lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
-                                        C.c_int64, C.c_void_p]
+    lib.fds_dw_split.restype = C.c_int32
+    lib.fds_dw_split.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.fds_dw_join.restype = C.c_int32
+    lib.fds_dw_join.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     # include/fds_surrogate.h
     P = C.c_void_p
     lib.fds_conv3x3.restype = C.c_int32

@@ -35,6 +35,28 @@ def join_dw(pairs):
     return pairs[:, 0].astype(np.float64) + pairs[:, 1].astype(np.float64)
 
 
+def upload_dw(torch, dev, vals, out=None):
+    """Host float64 values -> device (n, 2) float32 double words: the float64 copy
+    goes up (8 bytes per value, as the pairs would) and fds_dw_split splits it where
+    it lands, with the roundings of split_dw."""
+    v = torch.from_numpy(np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)).to(dev)
+    if out is None:
+        out = torch.empty((v.numel(), 2), dtype=torch.float32, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _capi.check(_capi.load().fds_dw_split(C.c_void_p(v.data_ptr()), C.c_void_p(out.data_ptr()),
+                                          v.numel(), stream))
+    return out
+
+
+def device_join_dw(torch, pairs):
+    """Device (n, 2) float32 double words -> device float64 values (fds_dw_join)."""
+    out = torch.empty(pairs.shape[0], dtype=torch.float64, device=pairs.device)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _capi.check(_capi.load().fds_dw_join(C.c_void_p(pairs.data_ptr()), C.c_void_p(out.data_ptr()),
+                                         pairs.shape[0], stream))
+    return out
+
+
 def _torch():
     import torch
     return torch
@@ -108,7 +130,7 @@ class StagEngine:
             if arr is None:
                 continue
             if self.field.precision == "dw":
-                self.coef_tensors[name] = torch.from_numpy(split_dw(arr)).to(dev)
+                self.coef_tensors[name] = upload_dw(torch, dev, arr)
                 continue
             self.coef_tensors[name] = torch.from_numpy(
                 np.ascontiguousarray(arr, dtype=np.float64)).to(dev).to(tc)
@@ -187,7 +209,7 @@ class StagEngine:
                 if k == 0 and off:
                     vals = vals - off
                 if dword:
-                    bufs[0].copy_(torch.from_numpy(split_dw(vals)).to(dev))
+                    upload_dw(torch, dev, vals, out=bufs[0])
                 else:
                     bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
                 comp._where = "both"
@@ -197,7 +219,7 @@ class StagEngine:
         torch = _torch()
         b = self.buffers[name][0]
         if self.field.precision == "dw":
-            v = b[:, 0].to(torch.float64) + b[:, 1].to(torch.float64)
+            v = device_join_dw(torch, b)
         else:
             v = b.to(dtype=torch.float64)
         if name == self.field._stag_components[0] and self.offset:
@@ -207,7 +229,7 @@ class StagEngine:
     def download(self, name):
         bufs = self.buffers[name]
         if self.field.precision == "dw":
-            v = join_dw(bufs[0].detach().to("cpu").numpy())
+            v = device_join_dw(_torch(), bufs[0]).to("cpu").numpy()
         else:
             v = bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
         if name == self.field._stag_components[0] and self.offset:

@@ -326,3 +326,17 @@ def test_batch_graph_replay(gpu):
     for fa, fb in zip(a, b):
         for name in fa._stag_components:
             assert torch.equal(fa._engine().buffers[name][0], fb._engine().buffers[name][0]), name
+
+
+def test_device_split_and_join_match_the_host(gpu):
+    """fds_dw_split / fds_dw_join produce the bits of split_dw / join_dw."""
+    import torch
+    from pyfds_gb300._engine import device_join_dw, join_dw, split_dw, upload_dw
+    rng = np.random.default_rng(12)
+    x = np.concatenate([rng.standard_normal(100001) * 10.0 ** rng.integers(-30, 30, 100001),
+                        [0.0, -0.0, 1.0, 3e38, -1e-40]])
+    dev = torch.device("cuda", 0)
+    pairs = upload_dw(torch, dev, x)
+    assert np.array_equal(pairs.cpu().numpy().view(np.uint32), split_dw(x).view(np.uint32))
+    back = device_join_dw(torch, pairs).cpu().numpy()
+    assert np.array_equal(back.view(np.uint64), join_dw(split_dw(x)).view(np.uint64))
