@@ -24,7 +24,11 @@ class StagField:
       exact:     float64 only; evaluate in the reference's operation order without
                  fused multiply-adds (bit-identical to scipy on x86-64).
       tile:      (x, y) cells per CTA for lossless 2-D fields, one of
-                 ``_capi.tile_menu()`` (default: the kernel's 64 x 16).
+                 ``_capi.tile_menu()`` (default: 64 x 16; double words 64 x 12).
+    The attribute ``stages`` selects one step per tile (1), the persistent two-stage
+    pipeline (2) or two steps per tile and launch (3, lossless 2-D fields); 0 (the
+    default) lets the engine choose (two steps per tile for float32 and double-word
+    acoustic fields and for batches).
     """
 
     _stag_family = None
@@ -40,7 +44,9 @@ class StagField:
         self.precision = precision
         self.exact = bool(exact)
         self.tile = tuple(tile) if tile is not None else None
-        self.stages = 0  # 0: automatic; 1 or 2 staging buffers (see FdsStagProblem)
+        # 0: automatic (StagEngine.stages); 1: one step per tile and launch; 2: the
+        # persistent two-stage pipeline; 3: two steps per tile (see FdsStagProblem)
+        self.stages = 0
         # float32 thermal fields store T - potential_offset (None: the mean initial
         # temperature at the first launch); double-word ones when it is set
         self.potential_offset = None

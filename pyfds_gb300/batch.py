@@ -21,6 +21,9 @@ class BatchRunner:
     """Device-side plan of one batched run of ``num_steps`` steps."""
 
     def __init__(self, fields, num_steps, tile=None, stages=None):
+        """``tile`` / ``stages`` override the fields' own (None: keep them; a field
+        stage of 0 lets the engine choose, two steps per tile where the tile has a
+        two-step kernel)."""
         if not fields:
             raise ValueError("empty batch")
         self.torch = require_cuda()

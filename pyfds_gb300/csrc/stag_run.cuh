@@ -255,7 +255,8 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   const bool exact = (prob->flags & FDS_FLAG_EXACT) != 0;
   const bool flow = (prob->flags & FDS_FLAG_FLOW) != 0;
   // stages: 0 (automatic) and 1 = one CTA per tile; 2 = the persistent two-stage
-  // pipeline (built for the tile menu; measured slower on GB300 for one field)
+  // pipeline (built for the tile menu; measured slower on GB300 for one field);
+  // 3 = two steps per tile and launch (stag_tb2_kernel; the host picks it)
   StagLaunch<TP, TF, TC> fn = nullptr;
   const bool two_step = prob->stages == 3;
   if (two_step) {
