@@ -368,6 +368,24 @@ def test_nonlinear_1d_vs_reference(gpu, exact):
         check_signals(sig, g, prefix, comps, bitwise)
 
 
+def test_nonlinear_1d_additive_velocity_bound_at_tile_seams(gpu):
+    """Additive velocity sources on cells where 64-cell tiles meet: the tile left of a
+    seam also holds the cell (as its halo), and each source must still be added once
+    per step (bit for bit the oracle in exact mode)."""
+    spec = S.nonlinear_scenario(5, "Acoustic2ndOrder1D", 300, steps=40)
+    t = np.arange(spec["nt"]) * spec["dt"]
+    spec["bounds"]["velocity"].append({"indices": [64, 128, 129],
+                                       "value": 1e-9 * np.sin(2e5 * t), "additive": True})
+    st_o, sg_o = O.simulate(spec, spec["steps"])
+    f = build_field(spec, exact=True)
+    f.simulate(spec["steps"])
+    st, sig = field_results(f)
+    for c in st_o:
+        assert np.array_equal(st[c], st_o[c]), c
+        for x, y in zip(sig[c], sg_o[c]):
+            assert np.array_equal(x, y), c
+
+
 def test_nonlinear_1d_sim_step_loop_equals_simulate(gpu):
     spec = S.nonlinear_scenario(77, "Acoustic2ndOrder1D", 300, steps=25)
     a = build_field(spec)
