@@ -32,7 +32,9 @@
 extern "C" {
 #endif
 
-#define FDS_ABI_VERSION 2
+/* 3: FdsBoundGroup.primary (was padding; kernels that apply bounds to global arrays
+ *    read it), FdsStagProblem.stages = 3, FDS_PREC_DW, fds_dw_split / fds_dw_join */
+#define FDS_ABI_VERSION 3
 
 /* error codes */
 #define FDS_OK 0

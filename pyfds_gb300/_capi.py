@@ -12,7 +12,7 @@ import numpy as np
 
 from ._build import LIB_PATH
 
-FDS_ABI_VERSION = 2
+FDS_ABI_VERSION = 3
 
 FDS_OK = 0
 FDS_E_ARG = -1
