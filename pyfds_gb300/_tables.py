@@ -116,13 +116,22 @@ class TileGeometry:
         x0 = cell % self.nx
         y0 = cell // self.nx
         src0 = np.arange(cell.size)
-        kmin = -((self.tiles_x * self.tx + mr + self.nx) // self.nx) - 1
-        kmax = (ml + self.tiles_x * self.tx + self.nx) // self.nx + 1
-        own_t, own_p = self.owner(cell)
+        own_t0, own_p0 = self.owner(cell)
+        # ring columns of all tiles: -ml .. W - 1 + mr; alias k exists for a cell when
+        # x + k*nx falls there (k in {-1, 0, 1} unless the grid is narrower than that)
+        W = self.tiles_x * self.tx
+        kmin = -((ml + self.nx - 1) // self.nx)
+        kmax = (W - 1 + mr) // self.nx
         out_t, out_p, out_s, out_q = [], [], [], []
         for k in range(kmin, kmax + 1):
             X = x0 + k * self.nx
-            Y = y0 - k
+            sel = np.nonzero((X >= -ml) & (X <= W - 1 + mr))[0]
+            if sel.size == 0:
+                continue
+            X = X[sel]
+            Y = y0[sel] - k
+            src = src0[sel]
+            own_t, own_p = own_t0[sel], own_p0[sel]
             # tiles whose ring [t*tx - ml, t*tx + tx - 1 + mr] contains X: at most
             # ceil((ml + mr) / tx) + 1 consecutive tile columns (two for the kernel's
             # tiles; more for tiles narrower than the margins)
@@ -141,7 +150,7 @@ class TileGeometry:
                         (X[ok] - tx[ok] * self.tx) + self.ox
                     out_t.append(t)
                     out_p.append(pos)
-                    out_s.append(src0[ok])
+                    out_s.append(src[ok])
                     out_q.append(((t == own_t[ok]) & (pos == own_p[ok])).astype(np.int32))
         if not out_t:
             z = np.zeros(0, np.int64)
