@@ -665,6 +665,9 @@ def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
     torch.cuda.synchronize()
     step_kernel_ms = ev[2].elapsed_time(ev[3]) / nt  # per time step
     spl = 2 if eng.stages() == 3 else 1  # steps per launch
+    # the kernels' status word (a bounded wait that gave up leaves a tile's outputs
+    # unwritten): checked here because launch() alone does not
+    status = int(eng.status.item())
     rows = [r for o in plan["outs"] if o is not None for r in o.cpu().numpy().T]
     refs = [r for o in ref_outs if o is not None for r in o.T]
     top = max((float(np.linalg.norm(r)) for r in refs), default=0.0)
@@ -688,7 +691,8 @@ def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
             "launch_ms": step_kernel_ms * spl, "steps_per_launch": spl, "achieved_gbs": achieved,
             "hbm_frac": achieved / peak if achieved and peak else None,
             "max_rel_l2_vs_f64": worst, "unreached_outputs": unreached,
-            "unreached_max_abs_vs_largest": worst_abs, "nonfinite_outputs": nonfinite}
+            "unreached_max_abs_vs_largest": worst_abs, "nonfinite_outputs": nonfinite,
+            "kernel_status": status}
 
 
 def run_ours(args):
@@ -745,6 +749,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     # time per step of the step kernel (two steps per launch with stages 3)
     step_kernel_ms = ev2.elapsed_time(ev3) / nt
+    kernel_status = int(eng.status.item()) if eng.status is not None else 0
+    if kernel_status:
+        raise RuntimeError("a kernel reported status 0x%x during the timed runs" % kernel_status)
     spl = 2 if eng.stages() == 3 else 1  # steps per launch
     launch_ms = step_kernel_ms * spl
     ref_outs = [o.cpu().numpy() if o is not None else None for o in plan["outs"]]
