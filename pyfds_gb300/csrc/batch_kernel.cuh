@@ -27,20 +27,23 @@ __device__ __forceinline__ void load_core(StagCore<TP, TF, TC>* dst,
   for (int i = threadIdx.x; i < W; i += blockDim.x) d[i] = s[i];
 }
 
-// Dynamic shared memory of the batched kernel: staging buffers (carved for the
-// anisotropic layout, the larger one), one mbarrier per stage, one core copy.
+// Dynamic shared memory of the batched kernel: staging buffers, one mbarrier per
+// stage, one core copy. The buffers are carved for the isotropic layout (five
+// arrays) when every instance of the batch is isotropic, else for the anisotropic
+// one (seven): for 8-byte values that is the difference between two and four CTAs
+// per SM.
 template <class C, typename TP, typename TF, typename TC>
-__host__ __device__ constexpr size_t batch_smem_bytes() {
-  return C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(false) + 16 * C::STAGES +
+__host__ __device__ constexpr size_t batch_smem_bytes(bool all_iso) {
+  return C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(all_iso) + 16 * C::STAGES +
          round128(sizeof(StagCore<TP, TF, TC>));
 }
 
 template <class C, typename TP, typename TF, typename TC>
 __global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
     stag_batch_kernel(const StagArgs<TP, TF, TC>* __restrict__ descs, const int2* __restrict__ work,
-                      int nwork, const StepInfo si, int parity, int prefetch) {
+                      int nwork, const StepInfo si, int parity, int prefetch, int all_iso) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(false);
+  const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(all_iso != 0);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + C::STAGES * bytes);
   StagCore<TP, TF, TC>* core =
       reinterpret_cast<StagCore<TP, TF, TC>*>(smem_raw + C::STAGES * bytes + 16 * C::STAGES);

@@ -441,9 +441,19 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
   }
   if (!(mode & FDS_BATCH_LAUNCH)) return FDS_OK;
 
-  // launch configuration
-  const size_t smem = batch_smem_bytes<C, TP, TF, TC>();
-  static int optin = -1, nsm = -1, occ = -1;
+  // launch configuration: staging sized for the isotropic layout when every
+  // instance is isotropic (by == bx and ky == kx, as the descriptors record it)
+  bool all_iso = true;
+  for (int i = 0; i < count; ++i) {
+    const FdsCoefs& c = probs[i].coefs;
+    const void* by = c.by ? c.by : c.bx;
+    const void* ky = c.ky ? c.ky : c.kx;
+    all_iso = all_iso && by == c.bx && ky == c.kx;
+  }
+  const size_t smem = batch_smem_bytes<C, TP, TF, TC>(all_iso);
+  static int optin = -1, nsm = -1;
+  static int occ_by_iso[2] = {-1, -1};
+  int& occ = occ_by_iso[all_iso ? 1 : 0];
   static size_t attr = 0;
   if (optin < 0) {
     int dev = 0;
@@ -490,7 +500,8 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     const StepInfo si{step0 + s, step0, (s + take < nsteps) ? 1 : 0,
                       (store_flux || s + take == nsteps) ? 1 : 0, take};
     stag_batch_kernel<C, TP, TF, TC><<<grid, C::NT, smem, stream>>>(d_desc, d_work, (int)nwork, si,
-                                                                    launches & 1, prefetch);
+                                                                    launches & 1, prefetch,
+                                                                    all_iso ? 1 : 0);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "batch step: %s", cudaGetErrorString(e));
     s += take;
