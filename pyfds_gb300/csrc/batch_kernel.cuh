@@ -39,7 +39,7 @@ __host__ __device__ constexpr size_t batch_smem_bytes(bool all_iso) {
 }
 
 template <class C, typename TP, typename TF, typename TC>
-__global__ void __launch_bounds__(C::NT, C::MIN_BLOCKS)
+__global__ void __launch_bounds__(C::NT, C::batch_blocks(sizeof(TP)))
     stag_batch_kernel(const StagArgs<TP, TF, TC>* __restrict__ descs, const int2* __restrict__ work,
                       int nwork, const StepInfo si, int parity, int prefetch, int all_iso) {
   extern __shared__ __align__(128) unsigned char smem_raw[];

@@ -122,6 +122,12 @@ __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
 #ifndef FDS_BATCH_BLOCKS_256
 #define FDS_BATCH_BLOCKS_256 4
 #endif
+// two steps per tile in the batched kernel, 4-byte values: 5 (128.6 -> 136.2
+// Gcell/s against 4 on 256 layered instances); 8-byte values keep 4 (at 5 float64
+// spills, and their staging holds four CTAs anyway)
+#ifndef FDS_BATCH_TB2_BLOCKS_256_F32
+#define FDS_BATCH_TB2_BLOCKS_256_F32 5
+#endif
 
 // Variant switches of the tile kernel.
 template <int TX_, int TY_, int NT_, bool HAS_V_, bool MEMORY_, bool ABSORB_, bool AXI_,
@@ -148,6 +154,8 @@ struct StagCfg {
       STAGES == 2 ? 1 : (HAS_V ? (NT >= 512 ? 2 : FDS_BATCH_BLOCKS_256) : 2);
   // CTAs per SM of the single-field kernel for a potential of `psize` bytes per value
   // (`dword`: double-word float32 pairs)
+  // CTAs per SM of the batched kernel for values of `psize` bytes
+  static constexpr int batch_blocks(int psize) { return MIN_BLOCKS; }
   static constexpr int min_blocks(int psize, bool dword = false) {
     return STAGES == 2 ? 1
                        : (HAS_V ? (NT >= 512 ? 2
@@ -764,6 +772,9 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
 template <int TX_, int TY_, int NT_, bool MEMORY_>
 struct Tb2Cfg : StagCfg<TX_, TY_, NT_, true, MEMORY_, false, false, false, 1> {
   static constexpr bool TWO_STEP = true;
+  static constexpr int batch_blocks(int psize) {
+    return psize == 4 ? FDS_BATCH_TB2_BLOCKS_256_F32 : FDS_BATCH_BLOCKS_256;
+  }
   static constexpr int OY = 2;
   static constexpr int RY = TY_ + 4;
   static constexpr int RN = (TX_ + 8) * RY;
