@@ -74,13 +74,16 @@ void select_tma(StagArgs<TP, TF, TC>& a, StagTmaCache* tc, const void* const* st
   a.use_tma = 1;
 }
 
-// Launch one step. STAGES == 1: one CTA per tile. STAGES == 2: persistent CTAs,
-// as many as fit on the device at this variant's occupancy.
-template <class C, typename TP, typename TF, typename TC>
-int32_t launch_stag(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
-  const bool iso = a.iso != 0 || !C::HAS_V;
-  // the TMA barriers (8 bytes per stage) follow the buffers
-  const size_t smem = (size_t)C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(iso) + 16 * C::STAGES;
+// Device limits, the dynamic shared-memory attribute and the resident CTAs per SM of
+// one tile-kernel instantiation (KERNEL), cached per instantiation and staging layout
+// (isotropic or not). Returns FDS_OK or an error code.
+struct LaunchShape {
+  int nsm;  // SMs of the device
+  int occ;  // resident CTAs per SM at this shared-memory size
+};
+
+template <auto KERNEL>
+int32_t kernel_shape(size_t smem, int threads, bool iso, LaunchShape* out) {
   static int optin = -1, nsm = -1;
   static size_t attr_bytes = 0;
   static int occ[2] = {-1, -1};
@@ -91,27 +94,45 @@ int32_t launch_stag(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
   if (smem > (size_t)optin)
-    return set_error(FDS_E_SIZE, "tile %dx%d with %d stages needs %zu bytes of shared memory "
-                     "(device allows %d)", C::TX, C::TY, C::STAGES, smem, optin);
+    return set_error(FDS_E_SIZE, "tile needs %zu bytes of shared memory (device allows %d)", smem,
+                     optin);
   if (smem > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(stag_step_kernel<C, TP, TF, TC>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
     attr_bytes = smem;
   }
-  select_tma<C>(a, tc, tc ? tc->state : nullptr);
   int& o = occ[iso ? 1 : 0];
   if (o < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &o, stag_step_kernel<C, TP, TF, TC>, C::NT, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, KERNEL, threads, smem);
     if (e != cudaSuccess || o < 1) o = 1;
   }
+  out->nsm = nsm;
+  out->occ = o;
+  return FDS_OK;
+}
+
+// L2 prefetch distance of the one-stage TMA path: the tile 0.4 waves of resident CTAs
+// ahead (measured on the 2048^2 step against 0 to 2 waves: double words +6 %, float32
+// +5 %, float64 +1 %; two waves already lose)
+inline int32_t prefetch_distance(const LaunchShape& ls) {
+  return (int32_t)(0.4 * ls.occ * ls.nsm);
+}
+
+// Launch one step. STAGES == 1: one CTA per tile. STAGES == 2: persistent CTAs,
+// as many as fit on the device at this variant's occupancy.
+template <class C, typename TP, typename TF, typename TC>
+int32_t launch_stag(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
+  const bool iso = a.iso != 0 || !C::HAS_V;
+  // the TMA barriers (16 bytes per stage) follow the buffers
+  const size_t smem = (size_t)C::STAGES * stag_buffer_bytes<C, TP, TF, TC>(iso) + 16 * C::STAGES;
+  LaunchShape ls;
+  const int32_t rc = kernel_shape<stag_step_kernel<C, TP, TF, TC>>(smem, C::NT, iso, &ls);
+  if (rc != FDS_OK) return rc;
+  select_tma<C>(a, tc, tc ? tc->state : nullptr);
   int grid = a.ntiles;
-  if (C::STAGES > 1) grid = a.ntiles < o * nsm ? a.ntiles : o * nsm;
-  // one-stage TMA path: each CTA prefetches into L2 the region of the tile 0.4 waves
-  // of resident CTAs ahead (measured on the 2048^2 step against 0 to 2 waves:
-  // double words +6 %, float32 +5 %, float64 +1 %; two waves already lose)
-  a.prefetch = (C::STAGES == 1 && a.use_tma) ? (int32_t)(0.4 * o * nsm) : 0;
+  if (C::STAGES > 1) grid = a.ntiles < ls.occ * ls.nsm ? a.ntiles : ls.occ * ls.nsm;
+  a.prefetch = (C::STAGES == 1 && a.use_tma) ? prefetch_distance(ls) : 0;
   stag_step_kernel<C, TP, TF, TC><<<grid, C::NT, smem, s>>>(a);
   return FDS_OK;
 }
@@ -121,32 +142,11 @@ template <class C, typename TP, typename TF, typename TC>
 int32_t launch_tb2(StagArgs<TP, TF, TC>& a, cudaStream_t s, StagTmaCache* tc) {
   const bool iso = a.iso != 0;
   const size_t smem = stag_buffer_bytes<C, TP, TF, TC>(iso) + 16;
-  static int optin = -1, nsm = -1;
-  static size_t attr_bytes = 0;
-  static int occ[2] = {-1, -1};
-  if (optin < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
-  if (smem > (size_t)optin)
-    return set_error(FDS_E_SIZE, "two-step tile %dx%d needs %zu bytes of shared memory "
-                     "(device allows %d)", C::TX, C::TY, smem, optin);
-  if (smem > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(stag_tb2_kernel<C, TP, TF, TC>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
-    attr_bytes = smem;
-  }
+  LaunchShape ls;
+  const int32_t rc = kernel_shape<stag_tb2_kernel<C, TP, TF, TC>>(smem, C::NT, iso, &ls);
+  if (rc != FDS_OK) return rc;
   select_tma<C>(a, tc, tc ? tc->state : nullptr);
-  int& o = occ[iso ? 1 : 0];
-  if (o < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &o, stag_tb2_kernel<C, TP, TF, TC>, C::NT, smem);
-    if (e != cudaSuccess || o < 1) o = 1;
-  }
-  a.prefetch = a.use_tma ? (int32_t)(0.4 * o * nsm) : 0;
+  a.prefetch = a.use_tma ? prefetch_distance(ls) : 0;
   stag_tb2_kernel<C, TP, TF, TC><<<a.ntiles, C::NT, smem, s>>>(a);
   return FDS_OK;
 }
@@ -451,35 +451,14 @@ int32_t batch_run_variant(const FdsStagProblem* probs, FdsStagState* states,
     all_iso = all_iso && by == c.bx && ky == c.kx;
   }
   const size_t smem = batch_smem_bytes<C, TP, TF, TC>(all_iso);
-  static int optin = -1, nsm = -1;
-  static int occ_by_iso[2] = {-1, -1};
-  int& occ = occ_by_iso[all_iso ? 1 : 0];
-  static size_t attr = 0;
-  if (optin < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
-  if (smem > (size_t)optin)
-    return set_error(FDS_E_SIZE, "batched tile %dx%d needs %zu bytes of shared memory", C::TX,
-                     C::TY, smem);
-  if (smem > attr) {
-    e = cudaFuncSetAttribute(stag_batch_kernel<C, TP, TF, TC>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
-    attr = smem;
-  }
-  if (occ < 0) {
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stag_batch_kernel<C, TP, TF, TC>,
-                                                      C::NT, smem);
-    if (e != cudaSuccess || occ < 1) occ = 1;
-  }
+  LaunchShape ls;
+  const int32_t rs = kernel_shape<stag_batch_kernel<C, TP, TF, TC>>(smem, C::NT, all_iso, &ls);
+  if (rs != FDS_OK) return rs;
   int grid = (int)nwork;
-  if (C::STAGES > 1) grid = (int)std::min<int64_t>(nwork, (int64_t)occ * nsm);
+  if (C::STAGES > 1) grid = (int)std::min<int64_t>(nwork, (int64_t)ls.occ * ls.nsm);
   // one-stage: prefetch the work item 0.4 waves of resident CTAs ahead (as the
   // single-field kernel)
-  const int prefetch = C::STAGES == 1 ? (int)(0.4 * occ * nsm) : 0;
+  const int prefetch = C::STAGES == 1 ? prefetch_distance(ls) : 0;
   if (nsteps > 0) {
     stag_batch_prologue_kernel<TP, TF, TC><<<count, 256, 0, stream>>>(d_desc, count, step0);
     e = cudaGetLastError();
