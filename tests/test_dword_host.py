@@ -90,3 +90,40 @@ def test_potential_offset_policy(precision, explicit, expected):
                     if precision in ("f64", "f32", "dw") else "f64")
     g.potential_offset = 5.0
     assert StagEngine(g)._potential_offset() == 0.0  # acoustic: never
+
+
+@pytest.mark.parametrize("kind,precision,kwargs,stages,batched,expected", [
+    ("Acoustic2D", "f32", {}, 0, False, 3),       # float32: two steps per tile
+    ("Acoustic2D", "dw", {}, 0, False, 3),        # double-word acoustic: two steps
+    ("Thermal2D", "dw", {}, 0, False, 0),         # double-word thermal keeps one
+    ("Thermal2D", "f32", {}, 0, False, 3),
+    ("Acoustic2D", "f64", {}, 0, False, 0),       # float64 (FP64-bound) keeps one
+    ("Acoustic2D", "f64", {"exact": True}, 0, False, 0),
+    ("Acoustic2D", "f32", {}, 1, False, 1),       # an explicit choice stands
+    ("Acoustic2D", "f64", {}, 3, False, 3),
+    ("Acoustic2D", "f64", {}, 0, True, 3),        # batches: two steps for every precision
+    ("Thermal2D", "f32_t64", {}, 0, True, 0),     # ... with one potential/flux type
+    ("Acoustic2D", "f32", {}, 2, True, 2),
+    ("Acoustic1D", "f32", {}, 0, False, 0),       # 1-D: no two-step kernel
+])
+def test_automatic_stages(kind, precision, kwargs, stages, batched, expected):
+    """StagEngine.stages: the field's choice when set; otherwise two steps per tile
+    where it was measured faster and a two-step kernel exists (lossless 2-D, not
+    exact, no moving medium, a two-step tile)."""
+    from pyfds_gb300._engine import StagEngine
+    spec = S.random_scenario(6, kind, 40, None if kind.endswith("1D") else 20, steps=2,
+                             mu=False)
+    f = build_field(spec, precision=precision, **kwargs)
+    f.stages = stages
+    f.assemble_matrices()
+    assert StagEngine(f).stages(batched=batched) == expected
+
+
+def test_automatic_stages_needs_lossless_fields():
+    from pyfds_gb300._engine import StagEngine
+    spec = S.random_scenario(6, "Acoustic2D", 40, 20, steps=2, mu=True)
+    f = build_field(spec, precision="f32")
+    f.assemble_matrices()
+    assert f._stag_flags() & _capi.FLAG_ABSORB
+    assert StagEngine(f).stages() == 0
+    assert StagEngine(f).stages(batched=True) == 0
