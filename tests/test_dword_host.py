@@ -1,6 +1,7 @@
 """Host side of the double-word precision (precision="dw"), without a GPU: the
 float64 <-> (hi, lo) float32 split, the ABI constant, the argument check of the C
-ABI that rejects exact double words, and the temperature-offset policy."""
+ABI that rejects exact double words, the temperature-offset policy, and the engine's
+automatic choice between one and two steps per tile."""
 import ctypes as C
 import os
 import re
