@@ -792,6 +792,29 @@ __device__ __forceinline__ TP potential_new(const StagBuf<TP, TF, TC>& b, int ps
   return (TP)settle(acc);
 }
 
+// Calls f(pos, flat) for the slots of a W x H block of the region whose first cell is
+// (x0 + dx0, y0 + dy0), thread t taking slots t, t + NT, ...; the slot and flat index
+// advance incrementally (no division per slot).
+template <class C, int W, int H, typename F>
+__device__ __forceinline__ void for_block(int x0, int y0, int dx0, int dy0, int nx, F&& f) {
+  constexpr int NT = C::NT, RX = C::RX, DC = NT % W, DR = NT / W;
+  int col = (int)threadIdx.x % W;
+  const int row = (int)threadIdx.x / W;
+  int pos = (row + dy0 + C::OY) * RX + col + dx0 + C::OX;
+  int64_t flat = (int64_t)(y0 + dy0 + row) * nx + (x0 + dx0 + col);
+  for (int c = threadIdx.x; c < W * H; c += NT) {
+    f(pos, flat);
+    col += DC;
+    pos += DR * RX + DC;
+    flat += (int64_t)DR * nx + DC;
+    if (col >= W) {
+      col -= W;
+      pos += RX - W;
+      flat += nx - W;
+    }
+  }
+}
+
 // Step si.step on the ring around the tile, in place in the staged region.
 template <class C, typename TP, typename TF, typename TC>
 __device__ __forceinline__ void compute_ring(const StagCore<TP, TF, TC>& a, const StepInfo si,
@@ -804,18 +827,13 @@ __device__ __forceinline__ void compute_ring(const StagCore<TP, TF, TC>& a, cons
   // not staged, so those slots would otherwise hold stale shared memory, which the
   // potential update multiplies by a zero coefficient)
   constexpr int UW = TX + 3, UH = TY + 2, VW = TX + 2, VH = TY + 3;
-  for (int c = threadIdx.x; c < UW * UH; c += NT) {
-    const int lx = c % UW - 1, ly = c / UW - 1;
-    const int pos = (ly + OY) * RX + lx + OX;
-    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
-    b.U[pos] = (f >= 0 && f < a.n) ? flux_new<C, true>(a, b.P, b.U, b.Bx, pos, f, 0) : TF(0);
-  }
-  for (int c = threadIdx.x; c < VW * VH; c += NT) {
-    const int lx = c % VW - 1, ly = c / VW - 1;
-    const int pos = (ly + OY) * RX + lx + OX;
-    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
-    b.V[pos] = (f >= 0 && f < a.n) ? flux_new<C, false>(a, b.P, b.V, b.By, pos, f, 0) : TF(0);
-  }
+  const int64_t n = a.n;
+  for_block<C, UW, UH>(x0, y0, -1, -1, a.nx, [&](int pos, int64_t f) {
+    b.U[pos] = (f >= 0 && f < n) ? flux_new<C, true>(a, b.P, b.U, b.Bx, pos, f, 0) : TF(0);
+  });
+  for_block<C, VW, VH>(x0, y0, -1, -1, a.nx, [&](int pos, int64_t f) {
+    b.V[pos] = (f >= 0 && f < n) ? flux_new<C, false>(a, b.P, b.V, b.By, pos, f, 0) : TF(0);
+  });
   __syncthreads();
   apply_bound_groups<NT>(a.tab[1], tile, b.U, a.pool, si.step);
   apply_bound_groups<NT>(a.tab[2], tile, b.V, a.pool, si.step);
@@ -824,12 +842,9 @@ __device__ __forceinline__ void compute_ring(const StagCore<TP, TF, TC>& a, cons
   write_probes<NT>(a.tab[2], tile, b.V, si.step - si.step0);
   // potential of step si.step + 1: each slot reads only its own old value
   constexpr int PW = TX + 2, PH = TY + 2;
-  for (int c = threadIdx.x; c < PW * PH; c += NT) {
-    const int lx = c % PW - 1, ly = c / PW - 1;
-    const int pos = (ly + OY) * RX + lx + OX;
-    const int64_t f = (int64_t)(y0 + ly) * a.nx + (x0 + lx);
-    if (f >= 0 && f < a.n) b.P[pos] = potential_new<C>(b, pos);
-  }
+  for_block<C, PW, PH>(x0, y0, -1, -1, a.nx, [&](int pos, int64_t f) {
+    if (f >= 0 && f < n) b.P[pos] = potential_new<C>(b, pos);
+  });
   __syncthreads();
   apply_bound_groups<NT>(a.tab[0], tile, b.P, a.pool, si.step + 1);
   __syncthreads();
