@@ -30,13 +30,14 @@ __global__ void __launch_bounds__(256) dw_join_kernel(const float2* __restrict__
 }
 
 int grid_for(int64_t n) {
-  static int nsm = 0;
-  if (nsm == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (nsm < 1) nsm = 1;
-  }
+  // SM count of the first device used (any value gives correct grid-stride loops)
+  static const int nsm = []() {
+    int dev = 0, count = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 1;
+    return count < 1 ? 1 : count;
+  }();
   const int64_t blocks = (n + 255) / 256;
   return (int)(blocks < (int64_t)nsm * 8 ? blocks : (int64_t)nsm * 8);
 }

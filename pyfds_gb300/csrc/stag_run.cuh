@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <utility>
 #include <vector>
 
@@ -75,39 +76,56 @@ void select_tma(StagArgs<TP, TF, TC>& a, StagTmaCache* tc, const void* const* st
 }
 
 // Device limits, the dynamic shared-memory attribute and the resident CTAs per SM of
-// one tile-kernel instantiation (KERNEL), cached per instantiation and staging layout
-// (isotropic or not). Returns FDS_OK or an error code.
+// one tile-kernel instantiation (KERNEL), cached per instantiation, device and staging
+// layout (isotropic or not; the shared-memory size follows from it). Safe to call from
+// several host threads. Returns FDS_OK or an error code.
 struct LaunchShape {
   int nsm;  // SMs of the device
   int occ;  // resident CTAs per SM at this shared-memory size
 };
 
+constexpr int kMaxDevices = 64;
+
 template <auto KERNEL>
 int32_t kernel_shape(size_t smem, int threads, bool iso, LaunchShape* out) {
-  static int optin = -1, nsm = -1;
-  static size_t attr_bytes = 0;
-  static int occ[2] = {-1, -1};
-  if (optin < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  struct Entry {
+    int optin = -1, nsm = -1;
+    size_t attr_bytes = 0;  // dynamic shared memory the attribute allows so far
+    int occ[2] = {-1, -1};
+  };
+  static std::mutex mu;
+  static Entry cache[kMaxDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices)
+    return set_error(FDS_E_LAUNCH, "device %d: at most %d devices per process", dev, kMaxDevices);
+  std::lock_guard<std::mutex> lock(mu);
+  Entry& c = cache[dev];
+  if (c.optin < 0) {
+    int optin = -1, nsm = -1;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || optin < 1 || nsm < 1)
+      return set_error(FDS_E_LAUNCH, "device attributes: %s", cudaGetErrorString(e));
+    c.nsm = nsm;
+    c.optin = optin;
   }
-  if (smem > (size_t)optin)
+  if (smem > (size_t)c.optin)
     return set_error(FDS_E_SIZE, "tile needs %zu bytes of shared memory (device allows %d)", smem,
-                     optin);
-  if (smem > attr_bytes) {
-    cudaError_t e =
-        cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                     c.optin);
+  if (smem > c.attr_bytes) {
+    e = cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "smem attribute: %s", cudaGetErrorString(e));
-    attr_bytes = smem;
+    c.attr_bytes = smem;
   }
-  int& o = occ[iso ? 1 : 0];
+  int& o = c.occ[iso ? 1 : 0];
   if (o < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, KERNEL, threads, smem);
-    if (e != cudaSuccess || o < 1) o = 1;
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, KERNEL, threads, smem);
+    o = (e == cudaSuccess && n >= 1) ? n : 1;
   }
-  out->nsm = nsm;
+  out->nsm = c.nsm;
   out->occ = o;
   return FDS_OK;
 }

@@ -806,13 +806,14 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------------ host side
 
 int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
+  static const int n = []() {
+    int dev = 0, count = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
-      n = 148;
-  }
+        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        count <= 0)
+      return 148;
+    return count;
+  }();
   return n;
 }
 

@@ -70,18 +70,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
 
 // ---------------------------------------------------------------- host side
 
+// The driver's tensor-map encoder, looked up once (a static initialised under the
+// language's once-only guarantee, so concurrent first calls see the same result).
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
