@@ -252,10 +252,13 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
   const int threads = prob->tile_x < 256 ? ((prob->tile_x + 31) / 32) * 32 : 256;
   // every CTA waits for the others at the grid barriers: all must be resident
   int dev = 0, sms = 0, per_sm = 0, coop = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, threads, 0);
+  cudaError_t q = cudaGetDevice(&dev);
+  if (q == cudaSuccess) q = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (q == cudaSuccess) q = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (q == cudaSuccess)
+    q = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, threads, 0);
+  if (q != cudaSuccess)
+    return set_error(FDS_E_LAUNCH, "nonlinear 1-D residency query: %s", cudaGetErrorString(q));
   if (!coop || (int64_t)per_sm * sms < ntiles)
     return set_error(FDS_E_SIZE, "%d tiles cannot all be resident (%d per SM x %d SMs)", ntiles,
                      per_sm, sms);
