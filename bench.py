@@ -50,6 +50,24 @@ CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 1
 L2_BYTES = 129 * 2 ** 20
 
 
+def _workload_label(wname, count=None, nt=None):
+    """The workload string of a line's config, the same for both arms. For the
+    layered-media batch `count` and `nt` default to its builder's defaults."""
+    builder, kwargs, _ = WORKLOADS[wname]
+    if wname != "batched":
+        return "%s: %s" % (wname, builder)
+    if count is None or nt is None:
+        import inspect
+        from pyfds_gb300 import workloads
+        params = inspect.signature(getattr(workloads, builder)).parameters
+        defaults = {k: v.default for k, v in params.items()}
+        defaults.update(kwargs)
+        count = defaults["count"] if count is None else count
+        nt = defaults["nt"] if nt is None else nt
+    return ("batched: %d layered-media Acoustic2D instances, n in [128, 1024] log-uniform, "
+            "%d steps each" % (count, nt))
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -208,8 +226,9 @@ def run_reference(args):
             "ms_per_step": procs * cells * steps / (v * 1e9) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded workload generator)",
-            "config": {"workload": args.workload, "cells": cells, "precision": "f64",
-                       "parallelism": "replicas"},
+            "config": {"workload": _workload_label(args.workload), "cells": cells,
+                       "precision": "f64",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
             "cpu_baseline": {"value": v, "unit": "Gcell/s", "cores": procs, "kind": "port",
                              "sample": "%d time steps of the full-size workload per process, "
                                        "%d processes (one replica each), numpy oracle"
@@ -317,8 +336,7 @@ def run_batched(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"dw": "f32x2 (double-word)"}.get(args.precision, args.precision),
             "data": "synthetic (seeded layered media, no dataset)",
-            "config": {"workload": "batched: %d layered-media Acoustic2D instances, n in "
-                                   "[128, 1024] log-uniform, %d steps each" % (len(fields), nt),
+            "config": {"workload": _workload_label("batched", len(fields), nt),
                        "cells": cells, "time_steps_per_step": nt, "precision": args.precision,
                        "tile": "%dx%d" % tuple(tile), "stages": stages,
                        "launch": "one kernel per time step for all instances, whole run "
@@ -811,7 +829,7 @@ def run_ours(args):
             "dtype": {"f64": "f64", "f32": "f32", "f32_t64": "f32+f64",
                       "dw": "f32x2 (double-word)"}[args.precision],
             "data": "synthetic (seeded workload generator, no dataset)",
-            "config": {"workload": "%s: %s" % (args.workload, builder), "nx": field._nx,
+            "config": {"workload": _workload_label(args.workload), "nx": field._nx,
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
                        "precision": args.precision, "tile": "%dx%d" % (eng._geometry().tx, eng._geometry().ty),
                        "stages": eng.stages(),
