@@ -110,3 +110,19 @@ class Animator2D(Animator):
         if component is None:
             component = getattr(self.field, self.observed_component).values
         return np.reshape(component, (self.field.y.samples, self.field.x.samples))
+
+
+# SI prefixes of the axis labels, by factor (the standard table, as pyfds/gfx.py:422-440
+# uses it: yocto to yotta in steps of 10^3)
+prefixes = {float('1e%d' % (3 * k)): p
+            for k, p in zip(range(-8, 9), ('y', 'z', 'a', 'f', 'p', 'n', 'µ', 'm', '',
+                                           'k', 'M', 'G', 'T', 'P', 'E', 'Z', 'Y'))}
+
+
+def get_prefix(value):
+    """Metric prefix for an axis whose largest value is ``value`` (pyfds/gfx.py:406-419):
+    the smallest factor with ``value / factor < 1000``, the largest factor if none
+    qualifies (including NaN). Returns ``(prefix, factor)``."""
+    factors = sorted(prefixes)
+    factor = next((f for f in factors if value / f < 1e3), factors[-1])
+    return prefixes[factor], factor
