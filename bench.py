@@ -360,11 +360,15 @@ def run_batched(args):
         procs = os.cpu_count() or 1
         steps = CPU_SAMPLE_STEPS["batched"]
         vals, _ = cpu_sample("batched", steps, procs, repeats=1)
+        one, _ = cpu_sample("batched", steps, 1, repeats=1)
         line["cpu_baseline"] = {"value": vals[0], "unit": "Gcell/s", "cores": procs,
                                 "kind": "port",
                                 "sample": "%d time steps of one batch instance per process, "
                                           "%d processes (the first %d instances), numpy oracle"
-                                          % (steps, procs, procs)}
+                                          % (steps, procs, procs),
+                                "one_process": {"value": one[0], "unit": "Gcell/s", "cores": 1,
+                                                "sample": "%d time steps of instance 0 in one "
+                                                          "process" % steps}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -875,11 +879,16 @@ def run_ours(args):
         procs = os.cpu_count() or 1
         steps = CPU_SAMPLE_STEPS[args.workload]
         vals, _ = cpu_sample(args.workload, steps, procs, repeats=1)
+        one, _ = cpu_sample(args.workload, steps, 1, repeats=1)
         line["cpu_baseline"] = {"value": vals[0], "unit": "Gcell/s", "cores": procs,
                                 "kind": "port",
                                 "sample": "%d time steps of the full-size workload per process, "
                                           "%d processes (one replica each), numpy oracle"
-                                          % (steps, procs)}
+                                          % (steps, procs),
+                                # the oracle is single-threaded: the same sample in one process
+                                "one_process": {"value": one[0], "unit": "Gcell/s", "cores": 1,
+                                                "sample": "%d time steps of the full-size "
+                                                          "workload in one process" % steps}}
     print(json.dumps(line), flush=True)
     return 0
 
