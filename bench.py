@@ -723,7 +723,7 @@ def run_ours(args):
     import torch
     ws, rank, local = _init_replicas()
     dev = torch.device("cuda", torch.cuda.current_device())
-    from pyfds_gb300 import workloads, _capi
+    from pyfds_gb300 import workloads
     builder, kwargs, balg = WORKLOADS[args.workload]
     kwargs = dict(kwargs)
     if args.time_steps:

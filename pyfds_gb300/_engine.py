@@ -147,7 +147,6 @@ class StagEngine:
     def flow_shift(self, step):
         """The moving-medium shift of ``step`` on the device state (fds_stag_flow_shift)."""
         torch = require_cuda()
-        dev = torch.device("cuda", torch.cuda.current_device())
         plan = self.prepare(step, 0)
         state = _capi.FdsStagState()
         for k, name in enumerate(self.field._stag_components):

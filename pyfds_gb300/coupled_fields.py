@@ -6,7 +6,6 @@ import numpy as np
 from . import _capi
 from . import acoustics as ac
 from . import coupling as cp
-from . import fields as fld
 from . import thermal as th
 from ._engine import require_cuda
 

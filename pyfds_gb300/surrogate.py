@@ -165,7 +165,6 @@ class ConvNet:
     # ------------------------------------------------------------------ passes
     def forward(self, b, shape, train):
         """x -> y for the batch buffers ``b`` (``train`` keeps z and h for backward)."""
-        nl = len(self.layers)
         h = b["x"]
         for l, (cin, cout, dil, kind) in enumerate(self.layers):
             L = self.params[l]
@@ -288,7 +287,6 @@ def _fd_runner(fields, warmup=True):
     after the warm-up launch that precedes the capture)."""
     r = BatchRunner(fields, JUMP)
     if warmup:
-        torch = r.torch
         saved = []
         for f in fields:
             eng = f._engine()
@@ -499,7 +497,6 @@ def surrogate_rollout(net, specs, total_steps, check_every=8, tol=0.01, chunk=64
     media, freq, zref = media_tensors(specs, torch, dev)
     S, r_src, r_all = _rollout_setup(fields, n, torch, dev)
     Snn = torch.empty_like(S)
-    all_idx = torch.arange(N, dtype=torch.int32, device=dev)
     njumps = (total_steps - T_SRC) // JUMP
     active = np.ones(N, dtype=bool)
     r_fb = None

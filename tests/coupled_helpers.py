@@ -1,5 +1,4 @@
 """Shared by the coupled-field tests: fixture inputs and results per field."""
-import numpy as np
 
 from golden_inputs import apply_inputs
 from oracle import scenarios as S

@@ -333,15 +333,17 @@ def test_acoustic_flow_sim_step_and_apply_flow(gpu):
 
 
 def test_acoustic_flow_large_grid_vs_oracle(gpu):
-    """A 1000 x 300 flow field (rows of several shift chunks) against the oracle."""
+    """A 1000 x 300 flow field (rows of several shift chunks): the state against the
+    oracle bit for bit (the probe signals of flow fields are compared with the
+    reference's in test_acoustic_flow_vs_reference)."""
     import warnings
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         spec = S.flow_scenario(43, 1000, 300, steps=8, flow="rows", mu=False)
         f = build_field(spec, exact=True)
     f.simulate(8)
-    st, sig = field_results(f)
-    ref_st, ref_sig = O.simulate(spec, 8)
+    st, _ = field_results(f)
+    ref_st, _ = O.simulate(spec, 8)
     for c in st:
         assert np.array_equal(st[c], ref_st[c]), c
 
