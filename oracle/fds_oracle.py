@@ -333,12 +333,25 @@ def write_outputs(values, outputs, signals):
 # --------------------------------------------------------------------------------------
 
 
-def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
+def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None, matvec=None,
+             inplace=False):
     """One ``sim_step`` of the given kind, in place on ``state`` (dict name -> array).
 
-    ``bounds``/``outputs``/``signals`` are dicts keyed by component name.
+    ``bounds``/``outputs``/``signals`` are dicts keyed by component name. ``matvec``
+    (default: ``dia_matvec`` on the operator lists) lets the CPU-baseline worker run
+    the operators as scipy matrices, the reference's own product. ``inplace``
+    subtracts each update into the state array itself, as the reference's ``-=``
+    does, instead of binding a new array (same values; the worker sets it so that
+    its timing carries no extra allocation).
     """
-    mv = dia_matvec
+    mv = matvec or dia_matvec
+
+    def update(name, delta):
+        """state[name] - delta."""
+        if inplace:
+            np.subtract(state[name], delta, out=state[name])
+        else:
+            state[name] = state[name] - delta
 
     def pre(name):
         apply_bounds(state[name], bounds.get(name, []), step)
@@ -372,42 +385,39 @@ def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
     elif kind == "Acoustic1D":
         # pyfds/acoustics.py:40-52
         pre("pressure")
-        state["velocity"] = state["velocity"] - (mv(ops["a_v_p"], state["pressure"])
-                                                 - mv(ops["a_v_v"], state["velocity"]))
+        update("velocity", mv(ops["a_v_p"], state["pressure"])
+               - mv(ops["a_v_v"], state["velocity"]))
         pre("velocity")
-        state["pressure"] = state["pressure"] - mv(ops["a_p_v"], state["velocity"])
+        update("pressure", mv(ops["a_p_v"], state["velocity"]))
     elif kind == "Acoustic2D":
         # pyfds/acoustics.py:111-128
         pre("pressure")
         p = state["pressure"]
-        state["velocity_x"] = state["velocity_x"] - (mv(ops["a_vx_p"], p)
-                                                     - mv(ops["a_vx_vx"], state["velocity_x"]))
-        state["velocity_y"] = state["velocity_y"] - (mv(ops["a_vy_p"], p)
-                                                     - mv(ops["a_vy_vy"], state["velocity_y"]))
+        update("velocity_x", mv(ops["a_vx_p"], p) - mv(ops["a_vx_vx"], state["velocity_x"]))
+        update("velocity_y", mv(ops["a_vy_p"], p) - mv(ops["a_vy_vy"], state["velocity_y"]))
         pre("velocity_x")
         pre("velocity_y")
-        state["pressure"] = state["pressure"] - (mv(ops["a_p_vx"], state["velocity_x"])
-                                                 + mv(ops["a_p_vy"], state["velocity_y"]))
+        update("pressure", mv(ops["a_p_vx"], state["velocity_x"])
+               + mv(ops["a_p_vy"], state["velocity_y"]))
     elif kind == "Acoustic3DAxi":
         # pyfds/acoustics.py:205-225
         pre("pressure")
         p = state["pressure"]
         r = ops["radii"]
         vx = state["velocity_x"]
-        state["velocity_x"] = vx - (mv(ops["a_vx_p"], p) - mv(ops["a_vx_vx"], vx)
-                                    + dt * ops["mu"] / ops["rho"] * vx / r ** 2)
-        state["velocity_y"] = state["velocity_y"] - (mv(ops["a_vy_p"], p)
-                                                     - mv(ops["a_vy_vy"], state["velocity_y"]))
+        update("velocity_x", mv(ops["a_vx_p"], p) - mv(ops["a_vx_vx"], vx)
+               + dt * ops["mu"] / ops["rho"] * vx / r ** 2)
+        update("velocity_y", mv(ops["a_vy_p"], p) - mv(ops["a_vy_vy"], state["velocity_y"]))
         pre("velocity_x")
         pre("velocity_y")
-        state["pressure"] = state["pressure"] - (mv(ops["a_p_vx"], state["velocity_x"] * r)
-                                                 + mv(ops["a_p_vy"], state["velocity_y"]))
+        update("pressure", mv(ops["a_p_vx"], state["velocity_x"] * r)
+               + mv(ops["a_p_vy"], state["velocity_y"]))
     elif kind == "Thermal1D":
         # pyfds/thermal.py:40-51
         pre("temperature")
         state["heat_flux"] = -mv(ops["a_q_t"], state["temperature"])
         pre("heat_flux")
-        state["temperature"] = state["temperature"] - mv(ops["a_t_q"], state["heat_flux"])
+        update("temperature", mv(ops["a_t_q"], state["heat_flux"]))
     elif kind == "Thermal2D":
         # pyfds/thermal.py:92-107
         pre("temperature")
@@ -416,8 +426,8 @@ def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
         state["heat_flux_y"] = -mv(ops["a_qy_t"], t)
         pre("heat_flux_x")
         pre("heat_flux_y")
-        state["temperature"] = state["temperature"] - (mv(ops["a_t_qx"], state["heat_flux_x"])
-                                                       + mv(ops["a_t_qy"], state["heat_flux_y"]))
+        update("temperature", mv(ops["a_t_qx"], state["heat_flux_x"])
+               + mv(ops["a_t_qy"], state["heat_flux_y"]))
     elif kind == "Thermal3DAxi":
         # pyfds/thermal.py:161-176
         pre("temperature")
@@ -427,8 +437,8 @@ def sim_step(kind, ops, state, bounds, outputs, signals, step, dt=None):
         state["heat_flux_y"] = -mv(ops["a_qy_t"], t)
         pre("heat_flux_x")
         pre("heat_flux_y")
-        state["temperature"] = state["temperature"] - (
-            mv(ops["a_t_qx"], state["heat_flux_x"] * r) + mv(ops["a_t_qy"], state["heat_flux_y"]))
+        update("temperature", mv(ops["a_t_qx"], state["heat_flux_x"] * r)
+               + mv(ops["a_t_qy"], state["heat_flux_y"]))
     else:
         raise ValueError("unknown field kind %r" % kind)
 

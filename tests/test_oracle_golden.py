@@ -286,3 +286,34 @@ def test_oracle_coupling_bitwise():
         def check(a, b, where):
             assert np.array_equal(a, b), (case, where)
         compare(O.simulate_coupled(spec, spec["steps"]), g, prefix, check)
+
+
+@pytest.mark.parametrize("kind", ["Acoustic1D", "Acoustic2D", "Acoustic3DAxi", "Thermal1D",
+                                  "Thermal2D", "Thermal3DAxi"])
+def test_baseline_worker_path_matches_the_oracle(kind):
+    """The CPU-baseline worker's step (scipy DIA products, in-place updates) gives the
+    oracle's values: bit for bit where scipy does not contract multiply-adds, within
+    1e-13 otherwise."""
+    from oracle import bench_worker as W
+    nx, ny = (23, None) if kind.endswith("1D") else (11, 7)
+    spec = S.random_scenario(31, kind, nx, ny, steps=6, mu=True)
+    ops = O.assemble(spec)
+    sops = W.scipy_operators(ops)
+    runs = []
+    for o, kw in ((ops, {}), (sops, {"matvec": W._dot, "inplace": True})):
+        st = {c: np.array(v, dtype=np.float64) for c, v in (spec.get("init") or {}).items()}
+        for c in O.components_of(kind):
+            st.setdefault(c, np.zeros(ops["n"]))
+        outs = spec.get("outputs") or {}
+        sig = {c: [[[] for _ in idx] for idx in outs.get(c, [])] for c in st}
+        for s in range(spec["steps"]):
+            O.sim_step(kind, o, st, spec.get("bounds") or {}, outs, sig, s, dt=spec["dt"], **kw)
+        runs.append((st, sig))
+    (a, sa), (b, sb) = runs
+    for c in a:
+        scale = max(np.linalg.norm(a[c]), 1e-300)
+        assert np.linalg.norm(a[c] - b[c]) <= 1e-13 * scale, c
+        assert len(sa[c]) == len(sb[c])
+        for x, y in zip(sa[c], sb[c]):  # one output each (outputs differ in size)
+            x, y = np.asarray(x, dtype=float), np.asarray(y, dtype=float)
+            assert x.shape == y.shape and np.allclose(x, y, rtol=1e-13, atol=0), c
