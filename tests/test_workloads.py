@@ -1,9 +1,9 @@
 """The seeded synthetic workloads have the shapes, materials, regions, sources, probes
 and time steps of the configurations the benchmarks are quoted on: Acoustic1D water
 (1000 cells), Acoustic2D water with a steel block (2048^2), 256 layered-media
-instances, Acoustic3DAxi disc source (1024 x 4096) and Thermal2D aluminium/polymer
-(4096^2). Sizes are checked at full scale where building the spec is cheap; the oracle
-runs only the 1-D case. No GPU."""
+instances, Acoustic3DAxi disc source (1024 x 4096), Thermal2D aluminium/polymer
+(4096^2) and the surrogate's 256^2 layered media. Sizes are checked at full scale where
+building the spec is cheap; the oracle runs only the 1-D case. No GPU."""
 import numpy as np
 import pytest
 
@@ -146,3 +146,25 @@ def test_seeded_builders_are_deterministic(builder):
         assert x["outputs"] == y["outputs"]
         for (ia, _), (ib, _) in zip(x["materials"], y["materials"]):
             assert (ia is None and ib is None) or np.array_equal(ia, ib)
+
+
+def test_surrogate_media():
+    """Surrogate training / evaluation media: the layered kind at a fixed 256^2 grid,
+    the source cut to zero from step 704, per-cell c and rho maps consistent with the
+    material regions (the oracle's material vector)."""
+    specs = W.surrogate_media(12, seed=5)
+    assert len(specs) == 12
+    for s in specs:
+        n = s["nx"]
+        assert (n, s["ny"], s["nt"], s["t_src"]) == (256, 256, 4096, 704)
+        cs = [m["sound_velocity"] for _, m in s["materials"]]
+        assert 3 <= len(cs) <= 8 and np.isclose(s["dt"], 0.4 * s["dx"] / max(cs))
+        assert np.isclose(s["dx"], min(cs) / (20 * s["frequency"]))
+        assert 0.5e6 <= s["frequency"] <= 5e6
+        src = [b for b in s["bounds"]["pressure"] if b["additive"]][0]["value"]
+        assert np.all(src[704:] == 0) and np.any(src[:704] != 0)
+        c = O.material_vector(n * n, s["materials"], "sound_velocity")
+        rho = O.material_vector(n * n, s["materials"], "density")
+        assert np.array_equal(s["c_map"].reshape(-1), c)
+        assert np.array_equal(s["rho_map"].reshape(-1), rho)
+    assert W.surrogate_media(3, seed=5)[0]["frequency"] == specs[0]["frequency"]
