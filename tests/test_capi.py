@@ -80,10 +80,3 @@ def test_argument_errors_are_reported(lib):
     assert "coefficient" in _capi.last_error()
     with pytest.raises(_capi.FdsError):
         _capi.check(_capi.FDS_E_ARG)
-
-
-def test_integration_notes_name_every_entry_point():
-    """INTEGRATION.md, the binding guide, names every function the headers declare."""
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [n for n in declared_functions() if "`" + n not in doc and n + "(" not in doc]
-    assert not missing, missing
