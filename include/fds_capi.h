@@ -18,6 +18,10 @@
  *    default stream). Calls return after enqueueing; they do not synchronise.
  *  - Return value: 0 on success, a negative FDS_E* code on failure; the message
  *    of the last failure on the calling thread is available from fds_last_error.
+ *  - Calls may come from several host threads and for several devices of one
+ *    process, each on its own problem, state and stream (the device is the
+ *    calling thread's current one); fds_stag_batch_run_static is the exception
+ *    (one shared workspace, see there).
  *  - Flat cell index i = x + y * nx (pyfds/fields.py:377); a 1-D field has ny = 1.
  *    Neighbours are i +- 1 and i +- nx with NO break at row ends: only indices
  *    outside [0, nx*ny) are dropped, as in the reference's truncated DIA operators.
