@@ -1,0 +1,142 @@
+"""The package's host-side geometry against the live reference, where its source tree
+is available (skipped elsewhere): index and position lookups, point / line /
+rectangle / triangle / ellipse regions, and material vectors from random overlapping
+regions, on random 1-D and 2-D grids. Lookups snap to a grid point within an absolute
+10-eps radius and fail otherwise, so positions are drawn from the grid coordinates
+and the outcomes, failures included, must agree. No GPU."""
+import numpy as np
+import pytest
+
+from oracle.ref_loader import load_reference, reference_available
+from pyfds_gb300 import fields as ours
+from pyfds_gb300 import regions as our_reg
+
+pytestmark = pytest.mark.skipif(not reference_available(),
+                                reason="the reference source tree is not present")
+
+SEEDS = range(12)
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return load_reference()
+
+
+def _outcome(fn):
+    """('ok', value) or ('error', exception type name)."""
+    try:
+        v = fn()
+    except Exception as e:  # the same failure must occur on both sides
+        return ("error", type(e).__name__)
+    if hasattr(v, "indices"):
+        v = np.asarray(v.indices).reshape(-1).tolist()
+    elif isinstance(v, tuple):
+        v = tuple(float(x) for x in v)
+    elif isinstance(v, (np.floating, float)):
+        v = float(v)
+    return ("ok", v)
+
+
+def _agree(fo, fr):
+    a, b = _outcome(fo), _outcome(fr)
+    assert a == b, (a, b)
+    return a[0] == "ok"
+
+
+def _grids(ref, seed):
+    rng = np.random.default_rng(seed)
+    nx, ny = (int(v) for v in rng.integers(3, 40, size=2))
+    dx, dy = (float(v) for v in rng.uniform(0.01, 2.0, size=2))
+    args = (nx, dx, ny, dy, 10, 1.0, int(5))
+    return rng, ref.fields.Field2D(*args), ours.Field2D(*args)
+
+
+def _points(rng, f, k):
+    """k grid points (x, y) of field f."""
+    xs, ys = f.x.vector, f.y.vector
+    return [(float(xs[i]), float(ys[j]))
+            for i, j in zip(rng.integers(0, len(xs), k), rng.integers(0, len(ys), k))]
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_lookups_2d(ref, seed):
+    rng, r, o = _grids(ref, seed)
+    ok = 0
+    for p in _points(rng, r, 20):
+        ok += _agree(lambda: o.get_index(p), lambda: r.get_index(p))
+        i = r.get_index(p)
+        _agree(lambda: o.get_position(i), lambda: r.get_position(i))
+        _agree(lambda: o.get_point_region(p), lambda: r.get_point_region(p))
+    assert ok == 20
+    off = (float(r.x.vector[1]) * 0.5, float(r.y.vector[0]))    # between two grid points
+    assert not _agree(lambda: o.get_index(off), lambda: r.get_index(off))
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_regions_2d(ref, seed):
+    rng, r, o = _grids(ref, seed)
+    ok = 0
+    for _ in range(8):
+        (x0, y0), (x1, y1), (x2, y2) = _points(rng, r, 3)
+        line = (x0, y0, x1, y1)
+        ok += _agree(lambda: o.get_line_region(line), lambda: r.get_line_region(line))
+        rect = (x0, y0, x1 - x0, y1 - y0)                        # either sign
+        _agree(lambda: o.get_rect_region(rect), lambda: r.get_rect_region(rect))
+        tri = (x0, y0, x1, y1, x2, y2)
+        _agree(lambda: o.get_tri_region(tri), lambda: r.get_tri_region(tri))
+    ellipses = 0
+    ys = r.y.vector
+    for _ in range(8):
+        # the ellipse's y extent is looked up on the grid: centre_y +- r_y must be grid
+        # points, so r_y is a whole number of y steps that stays inside the grid
+        i, j = int(rng.integers(0, len(r.x.vector))), int(rng.integers(0, len(ys)))
+        k = int(rng.integers(0, min(j, len(ys) - 1 - j) + 1))
+        centre = (float(r.x.vector[i]), float(ys[j]))
+        radii = (float(rng.uniform(0.5, 6.0) * r.x.increment), float(ys[k]))
+        if radii[1] == 0:
+            continue
+        ellipses += _agree(lambda: o.get_ellipse_region(centre, radii),
+                           lambda: r.get_ellipse_region(centre, radii))
+        _agree(lambda: o.get_ellipse_region(centre, radii[1]),   # scalar: a circle
+               lambda: r.get_ellipse_region(centre, radii[1]))
+    assert ok == 8  # lines between grid points always resolve
+    assert ellipses >= 1
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_lookups_and_lines_1d(ref, seed):
+    rng = np.random.default_rng(100 + seed)
+    n, dx = int(rng.integers(3, 200)), float(rng.uniform(1e-4, 1.0))
+    r = ref.fields.Field1D(n, dx, 10, 1.0, int(5))
+    o = ours.Field1D(n, dx, 10, 1.0, int(5))
+    xs = r.x.vector
+    for k in rng.integers(0, n, 20):
+        x = float(xs[k])
+        assert _agree(lambda: o.get_index(x), lambda: r.get_index(x))
+        _agree(lambda: o.get_position(int(k)), lambda: r.get_position(int(k)))
+    for a, b in rng.integers(0, n, (6, 2)):
+        lo, hi = float(xs[min(a, b)]), float(xs[max(a, b)])
+        assert _agree(lambda: o.get_line_region((lo, hi)), lambda: r.get_line_region((lo, hi)))
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_material_vectors_2d(ref, seed):
+    rng, r, o = _grids(ref, seed)
+    added = 0
+    for _ in range(6):
+        (x0, y0), (x1, y1) = _points(rng, r, 2)
+        line = (x0, y0, x1, y1)
+        value = int(rng.integers(6, 100))
+        r.material_regions.append(ref.regions.MaterialRegion(r.get_line_region(line), value))
+        o.material_regions.append(our_reg.MaterialRegion(o.get_line_region(line), value))
+        added += 1
+        tri = (x0, y0, x1, y1) + _points(rng, r, 1)[0]
+        ro, oo = _outcome(lambda: r.get_tri_region(tri)), _outcome(lambda: o.get_tri_region(tri))
+        assert ro == oo
+        if ro[0] == "ok":
+            value = int(rng.integers(6, 100))
+            r.material_regions.append(ref.regions.MaterialRegion(r.get_tri_region(tri), value))
+            o.material_regions.append(our_reg.MaterialRegion(o.get_tri_region(tri), value))
+            added += 1
+    assert added >= 6
+    assert np.array_equal(o.material_vector('real'), r.material_vector('real'))
