@@ -1,7 +1,8 @@
 """The package's host-side geometry against the live reference, where its source tree
 is available (skipped elsewhere): index and position lookups, point / line /
-rectangle / triangle / ellipse regions, and material vectors from random overlapping
-regions, on random 1-D and 2-D grids. Lookups snap to a grid point within an absolute
+rectangle / triangle / ellipse regions, material vectors from random overlapping
+regions, and boundary application / output recording of a component with boundaries
+of every value form, on random grids. Lookups snap to a grid point within an absolute
 10-eps radius and fail otherwise, so positions are drawn from the grid coordinates
 and the outcomes, failures included, must agree. No GPU."""
 import numpy as np
@@ -140,3 +141,55 @@ def test_material_vectors_2d(ref, seed):
             added += 1
     assert added >= 6
     assert np.array_equal(o.material_vector('real'), r.material_vector('real'))
+
+
+def _random_boundaries(rng, n, steps, make_boundary, make_region):
+    """Boundaries of every value form over random index sets (duplicates included):
+    scalar, one signal for all points, one signal per point, [steps][points] array."""
+    out = []
+    for _ in range(int(rng.integers(2, 7))):
+        k = int(rng.integers(1, 6))
+        idx = rng.integers(0, n, k).tolist()
+        form = int(rng.integers(0, 4))
+        if form == 0:
+            value = float(rng.normal())
+        elif form == 1:
+            value = rng.normal(size=steps)
+        elif form == 2:
+            value = [rng.normal(size=steps) for _ in idx]
+        else:
+            value = rng.normal(size=(steps, k))
+        out.append(make_boundary(make_region(idx), value, bool(rng.integers(0, 2))))
+    return out
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_component_bounds_and_outputs(ref, seed):
+    """FieldComponent.apply_bounds / write_outputs on host arrays, step by step."""
+    rng = np.random.default_rng(300 + seed)
+    n, steps = int(rng.integers(5, 60)), 6
+    r = ref.fields.FieldComponent(n)
+    o = ours.FieldComponent(n)
+    init = rng.normal(size=n)
+    r.values, o.values = init.copy(), init.copy()
+    state = rng.bit_generator.state
+    r.boundaries = _random_boundaries(
+        rng, n, steps, lambda reg_, v, a: ref.regions.Boundary(reg_, v, a),
+        lambda idx: ref.regions.PointRegion(idx, None))
+    rng.bit_generator.state = state  # the same boundaries for both
+    o.boundaries = _random_boundaries(
+        rng, n, steps, lambda reg_, v, a: our_reg.Boundary(reg_, v, a),
+        lambda idx: our_reg.PointRegion(idx, None))
+    probe = rng.integers(0, n, 4).tolist()
+    r.outputs = [ref.regions.Output(ref.regions.PointRegion(probe, None))]
+    o.outputs = [our_reg.Output(our_reg.PointRegion(probe, None))]
+    for step in range(steps):
+        ro = _outcome(lambda: r.apply_bounds(step))
+        oo = _outcome(lambda: o.apply_bounds(step))
+        assert ro == oo
+        if ro[0] == "error":
+            return
+        assert np.array_equal(o.values, r.values), step
+        r.write_outputs()
+        o.write_outputs()
+    assert np.array_equal(np.asarray(o.outputs[0].signals), np.asarray(r.outputs[0].signals))
