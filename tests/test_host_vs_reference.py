@@ -1,8 +1,8 @@
 """The package's host-side geometry against the live reference, where its source tree
 is available (skipped elsewhere): index and position lookups, point / line /
 rectangle / triangle / ellipse regions, material vectors from random overlapping
-regions, and boundary application / output recording of a component with boundaries
-of every value form, on random grids. Lookups snap to a grid point within an absolute
+regions, boundary application / output recording of a component with boundaries of
+every value form, on random grids, and material objects. Lookups snap to a grid point within an absolute
 10-eps radius and fail otherwise, so positions are drawn from the grid coordinates
 and the outcomes, failures included, must agree. No GPU."""
 import numpy as np
@@ -193,3 +193,37 @@ def test_component_bounds_and_outputs(ref, seed):
         r.write_outputs()
         o.write_outputs()
     assert np.array_equal(np.asarray(o.outputs[0].signals), np.asarray(r.outputs[0].signals))
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_materials(ref, seed):
+    """Material objects: constructor defaults, the absorption coefficient derived from
+    the viscosities and heat capacities (and its setter), the thermal conductivity
+    (scalar or per direction), and the second-order material's defaults."""
+    import pyfds_gb300 as fds
+    rng = np.random.default_rng(500 + seed)
+    c, rho = rng.uniform(100, 6000), rng.uniform(1, 8000)
+    kw = {k: float(rng.uniform(0, 1e-2)) for k in ("shear_viscosity", "bulk_viscosity",
+                                                    "thermal_conductivity")}
+    kw.update(isobaric_heat_cap=float(rng.uniform(1, 5)), isochoric_heat_cap=float(rng.uniform(1, 5)))
+    for args in ({}, kw, {"absorption_coef": float(rng.uniform(0, 1e-2))}):
+        r, o = ref.AcousticMaterial(c, rho, **args), fds.AcousticMaterial(c, rho, **args)
+        assert o.absorption_coef == r.absorption_coef
+        assert (o.sound_velocity, o.density) == (r.sound_velocity, r.density)
+        a = float(rng.uniform(0, 1e-2))
+        r.absorption_coef, o.absorption_coef = a, a
+        assert o.absorption_coef == r.absorption_coef
+    conds = [float(rng.uniform(0.1, 300)),
+             tuple(float(v) for v in rng.uniform(0.1, 300, 2))]
+    for k in conds:
+        outs = [_outcome(lambda: m.ThermalMaterial(897.0, 2700.0, k).thermal_conductivity)
+                for m in (ref, fds)]
+        assert outs[0] == outs[1]
+        r, o = ref.ThermalMaterial(897.0, 2700.0, k), fds.ThermalMaterial(897.0, 2700.0, k)
+        for name in ("heat_capacity", "density"):
+            assert getattr(o, name) == getattr(r, name)
+    for d in (2.0, None):  # None: the reference derives it (and fails doing so)
+        outs = [_outcome(lambda: (lambda m: (m.d_rho_p, m.d_rho2_p))(
+                    mod.AcousticMaterial2ndOrder(d_rho_p=d, sound_velocity=c, density=rho)))
+                for mod in (ref, fds)]
+        assert outs[0] == outs[1], outs
