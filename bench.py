@@ -50,6 +50,15 @@ CPU_SAMPLE_STEPS = {"acoustic2d": 20, "acoustic1d": 2000, "axi": 8, "thermal": 1
 L2_BYTES = 129 * 2 ** 20
 
 
+def _l2_label(nbytes, what):
+    """How the timed steps stand to the L2 cache: inputs larger than L2 stream from
+    HBM on every step; a set that fits stays resident (no flush between steps)."""
+    mb, l2 = nbytes / 2 ** 20, L2_BYTES / 2 ** 20
+    if nbytes > L2_BYTES:
+        return "inputs larger than L2 (%s %.0f MB > %.0f MB)" % (what, mb, l2)
+    return "fits in L2 (%s %.2f MB <= %.0f MB; resident between steps, no flush)" % (what, mb, l2)
+
+
 def _workload_label(wname, count=None, nt=None):
     """The workload string of a line's config, the same for both arms. For the
     layered-media batch `count` and `nt` default to its builder's defaults."""
@@ -341,9 +350,8 @@ def run_batched(args):
                        "tile": "%dx%d" % tuple(tile), "stages": stages,
                        "launch": "one kernel per time step for all instances, whole run "
                                  "replayed from one CUDA graph",
-                       "l2": "inputs larger than L2 (%.0f MB of state)"
-                             % (cells * 6 * (8 if args.precision in ("f64", "dw") else 4)
-                                / 2 ** 20),
+                       "l2": _l2_label(cells * 6 * (8 if args.precision in ("f64", "dw")
+                                                    else 4), "state"),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
@@ -837,8 +845,7 @@ def run_ours(args):
                        "ny": field._ny, "cells": cells, "time_steps_per_step": nt,
                        "precision": args.precision, "tile": "%dx%d" % (eng._geometry().tx, eng._geometry().ty),
                        "stages": eng.stages(),
-                       "l2": "inputs larger than L2 (working set %.0f MB > %.0f MB)"
-                             % ((state_bytes * 2 + coef_bytes) / 2 ** 20, L2_BYTES / 2 ** 20),
+                       "l2": _l2_label(state_bytes * 2 + coef_bytes, "working set"),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -358,9 +358,12 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
  * No counterpart in the reference (pyfds has no GPU and no C interface).
  * - A batch whose workspace (fds_stag_batch_workspace_bytes) exceeds the maximum
  *   is rejected with FDS_E_SIZE.
- * - The first call on each device, with that device current, looks up the
- *   array's device address (cudaGetSymbolAddress); make that first call before
- *   any stream capture.
+ * - Every call looks up the array's device address on the current device
+ *   (cudaGetSymbolAddress, no allocation), so the address stays right after a
+ *   device reset. The first call on a device also loads the module: make it
+ *   before any stream capture.
+ * - A call whose stream is capturing is rejected with FDS_E_ARG (the call copies
+ *   its descriptors from host memory that it frees on return).
  * - Every call shares the one array: calls whose work overlaps on the GPU (other
  *   streams, other threads) race and must be serialised by the caller.
  */

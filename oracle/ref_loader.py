@@ -23,7 +23,11 @@ import types
 
 import numpy as np
 
-DEFAULT_REFERENCE_ROOT = os.environ.get("PYFDS_REFERENCE_ROOT", "/root/reference")
+# The reference tree is found through PYFDS_REFERENCE_ROOT, else as a directory
+# named ``reference`` beside this repository's checkout.
+_SIBLING = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(
+    os.path.abspath(__file__)))), "reference")
+DEFAULT_REFERENCE_ROOT = os.environ.get("PYFDS_REFERENCE_ROOT", _SIBLING)
 
 
 def reference_available(root=DEFAULT_REFERENCE_ROOT):

@@ -10,15 +10,18 @@
 //
 // The array below lives in every GPU that loads this library, for the lifetime of
 // the process (FDS_BATCH_STATIC_MAX_BYTES of device memory). Host code cannot use
-// the array's name as a device address, so the first call on each device (with
-// that device current) resolves its address with cudaGetSymbolAddress; that first
-// call should therefore come before any stream capture. All calls share the one
-// array and it keeps the last call's contents; nothing in it has to start at zero
-// (every call rewrites the descriptors and work list it reads). Two calls whose
-// work overlaps on the GPU (different streams, or different host threads) race on
-// the array and must be serialised by the caller.
-#include <mutex>
-
+// the array's name as a device address, so every call resolves the address on the
+// current device with cudaGetSymbolAddress (a lookup, no allocation). Resolving
+// it per call instead of caching it keeps the address right after a device reset
+// or a new primary context, which reloads this module at another address. The
+// first call on a device also loads the module, so make it before any stream
+// capture. A call made while its stream is capturing is rejected (FDS_E_ARG): the
+// call uploads its descriptors from host memory that is freed when it returns,
+// which a captured copy would read again at every replay. All calls share the one
+// array and it keeps the last call's contents; nothing in it has to start at
+// zero (every call rewrites the descriptors and work list it reads). Two calls
+// whose work overlaps on the GPU (different streams, or different host threads)
+// race on the array and must be serialised by the caller.
 #include "fds_capi.h"
 #include "fds_internal.h"
 
@@ -26,26 +29,34 @@ static __device__ __align__(256) unsigned char g_batch_scratch[FDS_BATCH_STATIC_
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (set up once).
+// Device address of the scratch array in the current device's context.
 int32_t scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fds::set_error(FDS_E_LAUNCH, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fds::set_error(FDS_E_ARG, "device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_batch_scratch);
-    if (e != cudaSuccess || !p)
-      return fds::set_error(FDS_E_LAUNCH, "cudaGetSymbolAddress(scratch): %s",
-                            cudaGetErrorString(e));
-    g_scratch_ptr[dev] = p;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_batch_scratch);
+  if (e != cudaSuccess || !p)
+    return fds::set_error(FDS_E_LAUNCH, "cudaGetSymbolAddress(scratch): %s",
+                          cudaGetErrorString(e));
+  *out = p;
+  return FDS_OK;
+}
+
+// FDS_OK unless `stream` is being captured into a graph (or its capture state
+// cannot be read, as for the legacy stream while another stream captures).
+int32_t require_not_capturing(cudaStream_t stream) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  const cudaError_t e = cudaStreamIsCapturing(stream, &st);
+  if (e == cudaErrorStreamCaptureImplicit || e == cudaErrorStreamCaptureUnsupported) {
+    (void)cudaGetLastError();
+    return fds::set_error(FDS_E_ARG, "stream capture state: %s (this entry point cannot be "
+                          "called during a stream capture)", cudaGetErrorString(e));
   }
-  *out = g_scratch_ptr[dev];
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fds::set_error(FDS_E_LAUNCH, "cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+  }
+  if (st != cudaStreamCaptureStatusNone)
+    return fds::set_error(FDS_E_ARG, "fds_stag_batch_run_static cannot be called while its "
+                          "stream is capturing (it uploads descriptors from host memory)");
   return FDS_OK;
 }
 
@@ -56,21 +67,21 @@ extern "C" int32_t fds_stag_batch_run_static(const FdsStagProblem* probs, FdsSta
                                              int64_t step0, int32_t nsteps, int32_t store_flux,
                                              void* stream) {
   if (!probs || count < 1) return fds::set_error(FDS_E_ARG, "null argument or empty batch");
-  if (probs[0].tile_x < 1 || probs[0].tile_y < 1)
-    return fds::set_error(FDS_E_ARG, "bad tile shape %dx%d", probs[0].tile_x, probs[0].tile_y);
-  int64_t tiles = 0;
-  for (int i = 0; i < count; ++i)
-    tiles += (int64_t)((probs[i].nx + probs[0].tile_x - 1) / probs[0].tile_x) *
-             ((probs[i].ny + probs[0].tile_y - 1) / probs[0].tile_y);
-  const size_t need = fds_stag_batch_workspace_bytes(count, tiles);
-  if (need > (size_t)FDS_BATCH_STATIC_MAX_BYTES)
-    return fds::set_error(FDS_E_SIZE,
-                          "batch of %d fields / %lld tiles needs %zu bytes of scratch; the "
-                          "built-in scratch holds %zu (use fds_stag_batch_run with a workspace)",
-                          count, (long long)tiles, need, (size_t)FDS_BATCH_STATIC_MAX_BYTES);
-  void* ws = nullptr;
-  const int32_t rc = scratch_address(&ws);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int32_t rc = require_not_capturing(s);
   if (rc != FDS_OK) return rc;
-  return fds_stag_batch_run(probs, states, tables, count, ws, FDS_BATCH_STATIC_MAX_BYTES, step0,
-                            nsteps, store_flux, FDS_BATCH_UPLOAD | FDS_BATCH_LAUNCH, stream);
+  void* ws = nullptr;
+  rc = scratch_address(&ws);
+  if (rc != FDS_OK) return rc;
+  // the size check is the workspace entry point's own (same tile shapes)
+  rc = fds_stag_batch_run(probs, states, tables, count, ws, FDS_BATCH_STATIC_MAX_BYTES, step0,
+                          nsteps, store_flux, FDS_BATCH_UPLOAD | FDS_BATCH_LAUNCH, stream);
+  if (rc == FDS_E_SIZE) {
+    char msg[384];
+    fds_last_error(msg, sizeof(msg));
+    return fds::set_error(FDS_E_SIZE,
+                          "%s; the built-in scratch holds %zu bytes (use fds_stag_batch_run "
+                          "with a workspace)", msg, (size_t)FDS_BATCH_STATIC_MAX_BYTES);
+  }
+  return rc;
 }

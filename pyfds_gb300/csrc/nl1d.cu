@@ -16,6 +16,7 @@
 // after the other); with FDS_FLAG_EXACT every operation is an unfused IEEE operation,
 // so the result is the reference's bit for bit except where the ideal-gas state
 // equation calls pow (the device pow and the host's libm may differ in the last bit).
+#include <algorithm>
 #include <utility>
 
 #include "fds_capi.h"
@@ -25,6 +26,8 @@ namespace fds {
 namespace {
 
 constexpr long long kBarrierLimit = 1ll << 22;
+// arrivals one launch may count on its 32-bit barrier counter
+constexpr int64_t kMaxBarrierArrivals = 0xfffffff0ll;
 
 template <bool EXACT>
 struct Ops {
@@ -49,6 +52,7 @@ struct NlArgs {
   int32_t* status;
   int n, tile, ntiles;
   int64_t step0;
+  int64_t row0;  // output row of this launch's first step (calls run in several launches)
   int32_t nsteps;
 };
 
@@ -85,8 +89,10 @@ __device__ void write_probes(const FdsCompTables& tb, int t, const double* x, in
 }
 
 // Grid-wide barrier number k (0-based) of this launch: every CTA adds one to the
-// counter and waits until it reaches (k + 1) * gridDim.x. Bounded: false if the wait
-// gave up.
+// counter and waits until it reaches (k + 1) * gridDim.x. The counter is zeroed before
+// each launch and a launch runs at most kMaxBarrierArrivals / gridDim.x barriers (the
+// host splits longer calls), so neither the counter nor the target wraps. Bounded:
+// false if the wait gave up.
 __device__ bool grid_barrier(unsigned* count, unsigned k) {
   __syncthreads();
   int ok = 1;
@@ -126,7 +132,7 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
     double* rn = a.r[(s & 1) ^ 1];
     apply_bounds<EXACT>(a.tab[0], t, p, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[0], t, p, s);
+    write_probes(a.tab[0], t, p, a.row0 + s);
     if (!grid_barrier(a.sync, k++)) break;
     // velocity: v - ((a_v_p p) / B [+ a_v_v2 v] - (a_v_v v) / B), B = rho0 + d
     for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
     __syncthreads();
     apply_bounds<EXACT>(a.tab[1], t, vn, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[1], t, vn, s);
+    write_probes(a.tab[1], t, vn, a.row0 + s);
     if (!grid_barrier(a.sync, k++)) break;
     // density: d - a_d_v ((d + rho0) v), forward difference: diagonals 0 (-f1), +1 (f1)
     for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
     __syncthreads();
     apply_bounds<EXACT>(a.tab[2], t, rn, a.pool, step);
     __syncthreads();
-    write_probes(a.tab[2], t, rn, s);
+    write_probes(a.tab[2], t, rn, a.row0 + s);
     // state equation (own cells)
     for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       const double d = rn[i];
@@ -222,8 +228,9 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
   }
   if (nsteps == 0) return FDS_OK;
   const int ntiles = (prob->n + prob->tile_x - 1) / prob->tile_x;
-  if ((int64_t)2 * nsteps * ntiles >= 0xffffffffll)
-    return set_error(FDS_E_SIZE, "too many steps x tiles for one call");
+  // steps per launch: two barriers per step, kMaxBarrierArrivals per launch
+  const int64_t per_launch = kMaxBarrierArrivals / (2 * (int64_t)ntiles);
+  if (per_launch < 1) return set_error(FDS_E_SIZE, "too many tiles (%d)", ntiles);
   NlArgs a{};
   a.p = (double*)st->cur[0];
   a.v[0] = (double*)st->cur[1];
@@ -263,13 +270,24 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
     return set_error(FDS_E_SIZE, "%d tiles cannot all be resident (%d per SM x %d SMs)", ntiles,
                      per_sm, sms);
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(prob->sync, 0, sizeof(uint32_t), s);
-  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "barrier reset: %s", cudaGetErrorString(e));
-  void* params[] = {&a};
-  e = cudaLaunchCooperativeKernel((const void*)fn, dim3(ntiles), dim3(threads), params, 0, s);
-  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "nonlinear 1-D launch: %s", cudaGetErrorString(e));
-  // velocity and density were ping-ponged once per step
-  if (nsteps & 1)
-    for (int k = 1; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+  for (int64_t done = 0; done < nsteps;) {
+    const int32_t m = (int32_t)std::min<int64_t>(per_launch, nsteps - done);
+    a.step0 = step0 + done;
+    a.row0 = done;
+    a.nsteps = m;
+    cudaError_t e = cudaMemsetAsync(prob->sync, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "barrier reset: %s", cudaGetErrorString(e));
+    void* params[] = {&a};
+    e = cudaLaunchCooperativeKernel((const void*)fn, dim3(ntiles), dim3(threads), params, 0, s);
+    if (e != cudaSuccess)
+      return set_error(FDS_E_LAUNCH, "nonlinear 1-D launch: %s", cudaGetErrorString(e));
+    // velocity and density were ping-ponged once per step
+    if (m & 1) {
+      std::swap(a.v[0], a.v[1]);
+      std::swap(a.r[0], a.r[1]);
+      for (int k = 1; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+    }
+    done += m;
+  }
   return FDS_OK;
 }

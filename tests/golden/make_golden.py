@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the unmodified reference.
 
-Run where the reference source tree is available (PYFDS_REFERENCE_ROOT, default
-/root/reference)::
+Run where the reference source tree is available (PYFDS_REFERENCE_ROOT, or a
+``reference`` directory beside the repository checkout)::
 
     python tests/golden/make_golden.py [--skip-large]
 
@@ -20,6 +20,9 @@ source is not modified. Fixtures:
   workloads (500 steps), outputs and final-state norms.
 - axi_disc_full_prefix.npz, thermal2d_4096_prefix.npz: the full-size axisymmetric
   and thermal workloads for their first 100 steps (--skip-large skips them).
+- axi_disc_full_1000.npz, thermal2d_4096_1000.npz: the same full-size workloads for
+  their first 1000 steps, every output (about 12 and 7 minutes of reference CPU
+  time; --skip-large skips them).
 - acoustic_flow.npz: AcousticFlow2D (moving medium) scenarios, oracle/scenarios.py
   ``flow_scenario``: per-row and scalar flows, periods 1..9, negative and zero flows.
 - coupling.npz: coupled fields (ThermoAcoustic1D with stepping 1 and 3,
@@ -219,6 +222,10 @@ def main():
                                             workloads.axi_disc_source(), False, steps=100),
         "thermal_prefix": lambda: make_workload(
             "thermal2d_4096_prefix.npz", workloads.thermal2d_two_materials(), False, steps=100),
+        "axi_1000": lambda: make_workload("axi_disc_full_1000.npz",
+                                          workloads.axi_disc_source(), False, steps=1000),
+        "thermal_1000": lambda: make_workload(
+            "thermal2d_4096_1000.npz", workloads.thermal2d_two_materials(), False, steps=1000),
         "acoustic2d": lambda: make_workload("acoustic2d_steel_2048.npz",
                                             workloads.acoustic2d_steel_block(), False),
     }

@@ -6,13 +6,17 @@ allocator: its workspace is a fixed array built into the library. This file runs
 last (pytest collects it after the others) and must also pass on its own in a
 fresh process. Both entry points are driven through the C ABI on the same
 fields, twice in a row, and must agree within the float64 bar of the other
-parity tests (relative L2 1e-12; in fact bit for bit, the kernels are the same).
+parity tests (relative L2 1e-12; in fact bit for bit, the kernels are the same);
+after the two calls the allocation-free run is also held to the oracle's
+trajectory at that bar. A call made while its stream is being captured into a
+CUDA graph is rejected (the call copies its descriptors from host memory).
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+from oracle import fds_oracle as O
 from oracle import scenarios as S
 from helpers import build_field, rel_l2
 
@@ -78,7 +82,7 @@ def _run(fields, step0, nsteps, static):
 
 
 def test_static_scratch_matches_workspace_entry_point(gpu):
-    _, ref_fields = _fields()
+    specs, ref_fields = _fields()
     _, st_fields = _fields()
     for step0, n in ((0, 11), (11, 13)):  # two calls in a row
         a = _run(ref_fields, step0, n, static=False)
@@ -86,6 +90,32 @@ def test_static_scratch_matches_workspace_entry_point(gpu):
         for x, y in zip(a, b):
             assert rel_l2(y, x) <= TOL
             assert np.array_equal(x, y)
+    # the allocation-free trajectory against the oracle's, 24 steps
+    for spec, y in zip(specs, b):
+        st_o, _ = O.simulate(spec, 24)
+        assert rel_l2(y, st_o["pressure"]) <= TOL
+
+
+def test_static_scratch_rejects_a_capturing_stream(gpu):
+    import torch
+    from pyfds_gb300 import _capi
+    lib = _capi.load()
+    _, fields = _fields()
+    plans = [f._engine().prepare(0, 1) for f in fields]
+    probs, states, tables = _structs(fields, plans)
+    side = torch.cuda.Stream()
+    scratch = torch.zeros(16, device="cuda")
+    graph = torch.cuda.CUDAGraph()
+    codes = []
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            scratch.add_(1.0)  # the capture holds one node
+            codes.append(lib.fds_stag_batch_run_static(
+                probs, states, tables, len(fields), 0, 1, 1,
+                C.c_void_p(side.cuda_stream)))
+    torch.cuda.synchronize()
+    assert codes == [_capi.FDS_E_ARG]
+    assert "captur" in _capi.last_error()
 
 
 def test_static_scratch_rejects_oversized_batches(gpu):
