@@ -604,6 +604,65 @@ def run_surrogate(args):
     return 0
 
 
+def run_surrogate_precision(args):
+    """What limits the surrogate's jump error: the tcgen05 kernels (bf16 storage of
+    activations and operands) against a float32 twin of the same network trained on
+    the same pairs in the same order with the same schedule (PyTorch convolutions,
+    TF32 off), and the twin trained on a loss over two chained jumps. Errors are the
+    rollout check's relative L2 on unseen media after 1 .. 8 chained jumps from the
+    first source-free snapshot; "no network" keeps the state unchanged."""
+    import torch
+    from pyfds_gb300 import surrogate as S
+    from pyfds_gb300 import surrogate_twin as T
+    torch.cuda.init()
+    n = 256
+    jump = args.surr_jump
+    data = S.generate_data(args.surr_instances, args.surr_snaps, seed=11, n=n, jump=jump)
+    ev = S.generate_data(args.surr_eval_media, 9, seed=99, n=n, jump=jump)
+    jumps = 8
+
+    def summary(err):
+        return {"median_per_jump": [float(np.median(err[:, j])) for j in range(err.shape[1])],
+                "p90_first_jump": float(np.percentile(err[:, 0], 90)),
+                "max_first_jump": float(np.max(err[:, 0])),
+                "within_1pct_first_jump": int((err[:, 0] <= 0.01).sum())}
+
+    with torch.no_grad():
+        s0, _ = T._normalise(ev.state[:, 0], ev.zref[:, None, None])
+        ident = []
+        for k in range(1, jumps + 1):
+            tk, _ = T._normalise(ev.state[:, k], ev.zref[:, None, None])
+            ident.append((torch.linalg.vector_norm((s0 - tk).flatten(1), dim=1)
+                           / torch.linalg.vector_norm(tk.flatten(1), dim=1)).cpu().numpy())
+        ident = np.stack(ident, axis=1)
+    line = {"study": "surrogate precision: bf16 tcgen05 kernels vs a float32 twin; %d pairs "
+                     "at %dx%d, K=%d; eval %d unseen media, chained jumps"
+                     % (len(data.pairs()), n, n, jump, ev.count),
+            "epochs": args.surr_epochs, "batch": args.surr_batch, "jump": jump,
+            "no_network": summary(ident)}
+    variants = [v for v in args.surr_variants.split(",") if v]
+    for v in variants:
+        torch.cuda.empty_cache()
+        if v == "bf16":
+            net = S.ConvNet(seed=0)
+            losses, wall = S.train(net, data, epochs=args.surr_epochs, batch=args.surr_batch,
+                                   lr=1e-3, seed=0, log_every=max(1, len(data.pairs())
+                                                                  // args.surr_batch))
+            err = S.evaluate_jumps(net, ev, jumps)
+            del net
+        else:
+            unroll = 2 if v == "fp32x2" else 1
+            tw = T.TwinNet(seed=0)
+            losses, wall = T.train(tw, data, epochs=args.surr_epochs, batch=args.surr_batch,
+                                   lr=1e-3, seed=0, unroll=unroll)
+            err = T.evaluate(tw, ev, jumps)
+            del tw
+        line[v] = dict(summary(err), train_s=wall, loss_last=losses[-1][1] if losses else None,
+                       loss_per_epoch=[l for _, l in losses])
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_coupling_study(args):
     """ThermoAcoustic1D (1000 cells, coupling every 3 steps, accumulated): the
     one-call library stepping against the reference's loop (fields stepped one by
@@ -696,7 +755,7 @@ def _double_word_leg(args, spec, nt, ref_outs, barrier, bytes_per_cell):
     ev[3].record(stream)
     torch.cuda.synchronize()
     step_kernel_ms = ev[2].elapsed_time(ev[3]) / nt  # per time step
-    spl = 2 if eng.stages() == 3 else 1  # steps per launch
+    spl = {3: 2, 4: nt}.get(eng.stages(), 1)  # steps per launch
     # the kernels' status word (a bounded wait that gave up leaves a tile's outputs
     # unwritten): checked here because launch() alone does not
     status = int(eng.status.item())
@@ -784,7 +843,10 @@ def run_ours(args):
     kernel_status = int(eng.status.item()) if eng.status is not None else 0
     if kernel_status:
         raise RuntimeError("a kernel reported status 0x%x during the timed runs" % kernel_status)
-    spl = 2 if eng.stages() == 3 else 1  # steps per launch
+    st_used = eng.stages()
+    # steps per launch: two with two steps per tile, every step of the call for the
+    # wavefront kernel (stages 4, one launch per simulate call), else one
+    spl = 2 if st_used == 3 else (nt if st_used == 4 else 1)
     launch_ms = step_kernel_ms * spl
     ref_outs = [o.cpu().numpy() if o is not None else None for o in plan["outs"]]
     dword = None
@@ -833,8 +895,14 @@ def run_ours(args):
     # of the coefficients per step) over the time per step; with two steps per launch
     # the kernel moves about half of that from DRAM (see "traffic", per launch)
     achieved = cells * bpc / (step_kernel_ms * 1e-3) / 1e9 if bpc else None
-    pkey = "%s_%s%s" % (args.workload, args.precision, "_tb2" if spl == 2 else "")
+    pkey = "%s_%s%s" % (args.workload, args.precision,
+                        {3: "_tb2", 4: "_wave"}.get(st_used, ""))
     traffic = _traffic_from_profiles(pkey)
+    if st_used == 4:
+        # the capture covers a shorter call: its DRAM bytes per step, scaled to this
+        # launch's steps (the traffic grows with the steps a launch runs)
+        per_step = _traffic_from_profiles(pkey, "traffic_bytes_per_step")
+        traffic = per_step * nt if per_step else None
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -857,7 +925,9 @@ def run_ours(args):
                                     "nonlinear1d": "nl1d_kernel (every step in one launch; the "
                                                    "field stays in L1/L2)"}.get(
                                         args.workload,
-                                        "stag_tb2_kernel" if spl == 2 else "stag_step_kernel"),
+                                        {3: "stag_tb2_kernel", 4: "stag_wave_kernel (every "
+                                         "step of the call in one launch)"}.get(
+                                            st_used, "stag_step_kernel")),
                          "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl},
             "clocks": clk.summary(),
             # per simulate(): a prologue, then per step (per two steps with stages 3)
@@ -865,11 +935,14 @@ def run_ours(args):
             # step's pressure bounds)
             "gpu_launches": int(args.steps * (3 * nt if args.workload == "flow" else
                                               1 if args.workload == "nonlinear1d" else
+                                              2 if st_used == 4 else
                                               (nt + spl - 1) // spl + 1))}
     if dword is not None:
         line["double_word"] = dword
-    dfma = _traffic_from_profiles(pkey, "dfma_per_launch")
-    if dfma and launch_ms:
+    # DFMA per time step (the same count for one and for every step per launch)
+    dfma = _traffic_from_profiles("%s_%s" % (args.workload, args.precision), "dfma_per_launch")
+    if dfma and launch_ms and spl != 2:
+        dfma *= spl
         # the FP64 pipe bounds the float64 step: its roofline beside the HBM one. Peak =
         # 2 DFMA per clock per SM (ncu's peak_sustained of the DFMA counter) x SMs x the
         # maximum SM clock
@@ -914,13 +987,13 @@ def main():
                     help="float64 lines: skip the double-word leg (the same workload in "
                          "precision='dw')")
     ap.add_argument("--tile", default="", help="tile shape XxY for lossless 2-D fields")
-    ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--stages", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="staging buffers per CTA (0: automatic)")
     ap.add_argument("--batch", type=int, default=0, help="instances of the batched workload")
     ap.add_argument("--autotune", action="store_true", help="autotune the batched tile shape")
     ap.add_argument("--study", default="",
                     choices=["", "precision", "axi", "thermal", "batched", "surrogate",
-                             "surrogate-iter", "coupling"],
+                             "surrogate-iter", "surrogate-precision", "coupling"],
                     help="print the precision study (float32 paths against float64) or the "
                          "learned-surrogate study instead")
     ap.add_argument("--surr-instances", type=int, default=625,
@@ -932,6 +1005,13 @@ def main():
     ap.add_argument("--surr-eval", type=int, default=512, help="unseen media of the rollout")
     ap.add_argument("--surr-steps", type=int, default=4096, help="time steps of the rollout")
     ap.add_argument("--surr-save", default="", help="save the trained weights (.npz)")
+    ap.add_argument("--surr-jump", type=int, default=64,
+                    help="surrogate-precision study: time steps per jump")
+    ap.add_argument("--surr-eval-media", type=int, default=64,
+                    help="surrogate-precision study: unseen media evaluated")
+    ap.add_argument("--surr-variants", default="bf16,fp32,fp32x2",
+                    help="surrogate-precision study: bf16 (the kernels), fp32 (twin), "
+                         "fp32x2 (twin, loss over two chained jumps)")
     ap.add_argument("--surr-load", default="", help="load trained weights instead of training")
     ap.add_argument("--time-steps", type=int, default=0,
                     help="override the workload's time steps per benchmark step (profiling)")
@@ -940,6 +1020,8 @@ def main():
         return run_reference(args)
     if args.study == "surrogate":
         return run_surrogate(args)
+    if args.study == "surrogate-precision":
+        return run_surrogate_precision(args)
     if args.study == "surrogate-iter":
         return run_surrogate_iter(args)
     if args.study == "coupling":

@@ -38,7 +38,7 @@ extern "C" {
 
 /* 3: FdsBoundGroup.primary (was padding; kernels that apply bounds to global arrays
  *    read it), FdsStagProblem.stages = 3, FDS_PREC_DW, fds_dw_split / fds_dw_join */
-#define FDS_ABI_VERSION 3
+#define FDS_ABI_VERSION 4
 
 /* error codes */
 #define FDS_OK 0
@@ -123,7 +123,12 @@ typedef struct FdsStagProblem {
                      prefetch the next tile while computing one (lossless 2-D variants);
                      3: two steps per tile and launch (lossless 2-D, non-exact, no
                      moving medium, not float32-with-float64-potential; tables in slot
-                     layout 2, see fds_stag_tile_menu) */
+                     layout 2, see fds_stag_tile_menu);
+                     4: every step of the call in one persistent launch (lossless 2-D,
+                     non-exact, no moving medium, default tile shape; slot layout 0):
+                     CTAs take (step, tile) items in order from a queue and wait,
+                     bounded, until the tile rows around their tile finished the
+                     previous step; needs FdsStagTables.sync */
   FdsCoefs coefs;
   double offset;  /* thermal float32 only: the temperature is stored as T - offset
                      (finer float spacing near a reference temperature); the flux
@@ -198,11 +203,18 @@ typedef struct FdsStagTables {
   int64_t pool_len;
   int32_t* status;    /* device int32 the kernels OR FDS_STATUS_* bits into, or NULL;
                          the caller zeroes it and reads it after the stream work */
+  uint32_t* sync;     /* stages 4 only: device scratch of fds_stag_sync_words() words
+                         (the library zeroes them before each launch); NULL otherwise */
+  int64_t sync_words; /* capacity of `sync` in 32-bit words */
 } FdsStagTables;
 
 /* Bits of FdsStagTables.status */
-#define FDS_STATUS_TMA_TIMEOUT 1 /* a tile's TMA copies did not land within the
-                                    bounded wait; that tile was not updated */
+#define FDS_STATUS_TMA_TIMEOUT 1 /* a bounded wait gave up (TMA copies that did not
+                                    land, or, with stages 4, tile rows of the previous
+                                    step that did not finish); that tile was not
+                                    updated and the state is not valid */
+#define FDS_STATUS_NONFINITE 2   /* the potential of the call's last step holds a
+                                    NaN or an infinity (the field diverged) */
 
 /* ABI version of the loaded library (FDS_ABI_VERSION). */
 int32_t fds_abi_version(void);
@@ -246,6 +258,11 @@ int32_t fds_stag_tile_menu(int32_t* tile_x, int32_t* tile_y, int32_t* layout, in
 int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
                      const FdsStagTables* tables, int64_t step0, int32_t nsteps,
                      int32_t store_flux, void* stream);
+
+/* 32-bit words of FdsStagTables.sync that a stages-4 run of `prob` needs (one
+ * work counter and one completion counter per row of tiles), or a negative error
+ * code. The replaced reference loop is the same as fds_stag_run's. */
+int64_t fds_stag_sync_words(const FdsStagProblem* prob);
 
 /* ---------------------------------------------------------------- nonlinear 1-D
  * IdealGas1D and Acoustic2ndOrder1D (pyfds/nonlinear_acoustics.py:10-171): pressure,
@@ -345,6 +362,18 @@ int32_t fds_stag_batch_run(const FdsStagProblem* probs, FdsStagState* states,
                            const FdsStagTables* tables, int32_t count, void* workspace,
                            size_t workspace_bytes, int64_t step0, int32_t nsteps,
                            int32_t store_flux, uint32_t mode, void* stream);
+
+/*
+ * Diagnostics: runs the kernels' bounded-wait helpers on waits that nothing
+ * completes, with `poll_limit` polls (1 .. 2^20): mode 0 an mbarrier that no copy or
+ * arrival targets (the TMA staging wait), mode 1 the device word `counter` (zero,
+ * never incremented; the wavefront kernel's tile-row wait). The wait gives up,
+ * FDS_STATUS_TMA_TIMEOUT is ORed into *status (device int32) and the kernel returns;
+ * no copy is left in flight. Tests the timeout path end to end without a fault.
+ * No counterpart in the reference (pyfds has no GPU and no bounded waits).
+ */
+int32_t fds_selftest_bounded_wait(int32_t mode, int32_t* status, const uint32_t* counter,
+                                  int64_t poll_limit, void* stream);
 
 /* Size of the scratch array built into the library for fds_stag_batch_run_static. */
 #define FDS_BATCH_STATIC_MAX_BYTES (8u << 20)

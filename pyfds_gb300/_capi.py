@@ -12,7 +12,7 @@ import numpy as np
 
 from ._build import LIB_PATH
 
-FDS_ABI_VERSION = 3
+FDS_ABI_VERSION = 4
 
 FDS_OK = 0
 FDS_E_ARG = -1
@@ -48,8 +48,10 @@ BOP_SIGNAL = 2
 
 # exported symbols, in header order
 EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
-                    "fds_stag_tile_menu", "fds_stag_run", "fds_stag_batch_workspace_bytes",
-                    "fds_stag_batch_run", "fds_stag_batch_run_static", "fds_stag_flow_shift",
+                    "fds_stag_tile_menu", "fds_stag_run", "fds_stag_sync_words",
+                    "fds_stag_batch_workspace_bytes",
+                    "fds_stag_batch_run", "fds_selftest_bounded_wait", "fds_stag_batch_run_static",
+                    "fds_stag_flow_shift",
                     "fds_nl1d_run", "fds_thermoacoustic_run", "fds_dw_split", "fds_dw_join",
                     # include/fds_surrogate.h
                     "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
@@ -87,10 +89,11 @@ class FdsCompTables(C.Structure):
 
 class FdsStagTables(C.Structure):
     _fields_ = [("comp", FdsCompTables * 3), ("pool", C.c_void_p), ("pool_len", C.c_int64),
-                ("status", C.c_void_p)]
+                ("status", C.c_void_p), ("sync", C.c_void_p), ("sync_words", C.c_int64)]
 
 
 STATUS_TMA_TIMEOUT = 1
+STATUS_NONFINITE = 2
 
 BATCH_UPLOAD = 1
 BATCH_LAUNCH = 2
@@ -156,6 +159,13 @@ class FdsError(RuntimeError):
         self.code = code
 
 
+class FieldDiverged(FloatingPointError):
+    """The potential after a ``simulate()`` call holds NaN or infinity: the time step
+    exceeds the explicit scheme's stability limit (the reference's ``is_stable()``,
+    pyfds/acoustics.py:54-63, would have said so). Raised after the call's outputs
+    are recorded and the field's step advanced, so the state can be inspected."""
+
+
 _lib = None
 
 
@@ -187,6 +197,8 @@ def load(path=None):
     lib.fds_stag_run.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                  C.POINTER(FdsStagTables), C.c_int64, C.c_int32, C.c_int32,
                                  C.c_void_p]
+    lib.fds_stag_sync_words.restype = C.c_int64
+    lib.fds_stag_sync_words.argtypes = [C.POINTER(FdsStagProblem)]
     lib.fds_stag_batch_workspace_bytes.restype = C.c_size_t
     lib.fds_stag_batch_workspace_bytes.argtypes = [C.c_int32, C.c_int64]
     lib.fds_stag_batch_run.restype = C.c_int32
@@ -194,6 +206,9 @@ def load(path=None):
                                        C.POINTER(FdsStagTables), C.c_int32, C.c_void_p,
                                        C.c_size_t, C.c_int64, C.c_int32, C.c_int32, C.c_uint32,
                                        C.c_void_p]
+    lib.fds_selftest_bounded_wait.restype = C.c_int32
+    lib.fds_selftest_bounded_wait.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                              C.c_void_p]
     lib.fds_stag_batch_run_static.restype = C.c_int32
     lib.fds_stag_batch_run_static.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                               C.POINTER(FdsStagTables), C.c_int32, C.c_int64,

@@ -8,6 +8,7 @@ uploads what the host changed, compiles the boundary/output tables, calls
 tensors; libfdsgpu.so only borrows the pointers.
 """
 import ctypes as C
+import warnings
 
 import numpy as np
 
@@ -18,6 +19,20 @@ PRECISIONS = {"f64": _capi.PREC_F64, "f32": _capi.PREC_F32, "f32_t64": _capi.PRE
               "dw": _capi.PREC_DW}
 
 _ALIGN = 256
+
+# What a diverged field (NaN or infinity in the potential after a call, reported by
+# the kernels' status word) does: "raise" FieldDiverged (a FloatingPointError),
+# "warn" (RuntimeWarning, as numpy does on invalid values) or "ignore".
+NONFINITE_ACTIONS = ("raise", "warn", "ignore")
+_nonfinite_action = "raise"
+
+
+def set_nonfinite_action(action):
+    """Choose what a diverged field does: "raise" (default), "warn" or "ignore"."""
+    global _nonfinite_action
+    if action not in NONFINITE_ACTIONS:
+        raise ValueError("action must be one of %s" % (NONFINITE_ACTIONS,))
+    _nonfinite_action = action
 
 
 def split_dw(vals):
@@ -107,6 +122,7 @@ class StagEngine:
         self.table_cache = None
         self.launches = 0
         self.status = None  # device int32: FDS_STATUS_* bits reported by the kernels
+        self.sync = None  # device int32 scratch of the wavefront run (stages 4)
         self.offset = None  # the potential is stored as value - offset (see potential_offset)
 
     # ------------------------------------------------------------------ dtypes
@@ -242,26 +258,43 @@ class StagEngine:
     TWO_STEP_AUTO = {("f32", _capi.FAMILY_ACOUSTIC), ("f32", _capi.FAMILY_THERMAL),
                      ("dw", _capi.FAMILY_ACOUSTIC)}
 
+    # precisions and families where every step of a call in one persistent launch
+    # (stages 4, the wavefront kernel) is the faster default: float64 acoustic fields,
+    # bound by the FP64 pipe, lose the wave tail and ramp of one launch per step
+    # (2048^2: 59.7 -> 64.0 Gcell/s; axisymmetric 1024 x 4096: 60.9 -> 65.1); thermal
+    # fields are faster with one launch per step (float64 68.6 vs 63.5, double words
+    # 95.7 vs 53.1), float32 and double-word acoustic fields with two steps per tile
+    WAVE_AUTO = {("f64", _capi.FAMILY_ACOUSTIC)}
+    WAVE_TILES = ((64, 16), (64, 12))
+
     def stages(self, batched=False):
         """FdsStagProblem.stages of the next launch: the field's ``stages`` when set;
-        for 0 (automatic) two steps per tile (3) where that is the faster default and
-        the variant has a two-step kernel (lossless 2-D, not exact, no moving medium,
-        a two-step tile), else 0. Batched runs take the field's 1, 2 or 3 (the
-        autotuner's choice); for 0 two steps per tile whenever the tile has a
-        two-step kernel (measured faster for every precision in the batched kernel:
-        float32 +22 %, double words +20 %, float64 +8 %)."""
+        for 0 (automatic) every step in one persistent launch (4) or two steps per
+        tile (3) where that is the faster default and the variant has such a kernel
+        (lossless 2-D, not exact, no moving medium, a tile with that kernel), else 0.
+        Batched runs take the field's 1, 2 or 3 (the autotuner's choice; 4 counts as
+        0); for 0 two steps per tile whenever the tile has a two-step kernel
+        (measured faster for every precision in the batched kernel: float32 +22 %,
+        double words +20 %, float64 +8 %)."""
         f = self.field
         st = int(getattr(f, "stages", 0) or 0)
+        if batched and st == 4:
+            st = 0
         if st:
             return st
         flags = f._stag_flags()
         lossless_2d = (flags & _capi.FLAG_HAS_V) and not (
             flags & (_capi.FLAG_ABSORB | _capi.FLAG_EXACT | _capi.FLAG_FLOW))
-        if not lossless_2d or self._tile_shape() not in _capi.TWO_STEP_TILES:
+        if not lossless_2d:
             return 0
+        tile = self._tile_shape()
         if batched:
-            return 3 if f.precision != "f32_t64" else 0
-        return 3 if (f.precision, f._stag_family) in self.TWO_STEP_AUTO else 0
+            return 3 if f.precision != "f32_t64" and tile in _capi.TWO_STEP_TILES else 0
+        if (f.precision, f._stag_family) in self.WAVE_AUTO and tile in self.WAVE_TILES:
+            return 4
+        if tile in _capi.TWO_STEP_TILES and (f.precision, f._stag_family) in self.TWO_STEP_AUTO:
+            return 3
+        return 0
 
     def _tile_shape(self):
         f = self.field
@@ -391,6 +424,15 @@ class StagEngine:
             self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         tstruct = self._tables_struct(tabs, outs, nsteps)
         tstruct.status = self.status.data_ptr()
+        if prob.stages == 4:
+            # scratch counters of the wavefront run (zeroed by the library per launch)
+            words = int(_capi.load().fds_stag_sync_words(C.byref(prob)))
+            if words < 0:
+                _capi.check(words)
+            if self.sync is None or self.sync.numel() < words:
+                self.sync = torch.zeros(words, dtype=torch.int32, device=dev)
+            tstruct.sync = self.sync.data_ptr()
+            tstruct.sync_words = self.sync.numel()
         return {"prob": prob, "tabs": tabs, "outs": outs, "tstruct": tstruct,
                 "step0": int(step0), "nsteps": int(nsteps), "geo": geo}
 
@@ -422,14 +464,17 @@ class StagEngine:
 
     def finish(self, plan):
         """Copy the output buffers to the host and append them to Output.signals;
-        raise if a kernel reported a failed bounded wait."""
+        raise if a kernel reported a failed bounded wait. Returns True when the
+        kernels reported a non-finite potential (see ``report_nonfinite``)."""
         f = self.field
         st = int(self.status.item())
         if st:
             self.status.zero_()
+        if st & _capi.STATUS_TMA_TIMEOUT:
             raise _capi.FdsError(_capi.FDS_E_TIMEOUT,
-                                 "a kernel reported status 0x%x (TMA copies did not land within "
-                                 "the bounded wait); the field state is not valid" % st)
+                                 "a kernel reported status 0x%x (a bounded wait gave up: TMA "
+                                 "copies that did not land, or tiles of the previous step that "
+                                 "did not finish); the field state is not valid" % st)
         for k, name in enumerate(f._stag_components):
             out_t = plan["outs"][k]
             if out_t is None:
@@ -445,11 +490,25 @@ class StagEngine:
                 else:
                     for j, sig in enumerate(out.signals[:npts]):
                         sig.extend(block[:, j])
+        return bool(st & _capi.STATUS_NONFINITE)
+
+    def report_nonfinite(self, step):
+        """Act on a diverged field as set_nonfinite_action chose (after the caller
+        advanced the field's step to ``step``)."""
+        msg = ("%s diverged: its %s holds NaN or infinity after step %d (the time step "
+               "exceeds the explicit scheme's stability limit)"
+               % (type(self.field).__name__, self.field._stag_components[0], step - 1))
+        if _nonfinite_action == "raise":
+            raise _capi.FieldDiverged(msg)
+        if _nonfinite_action == "warn":
+            warnings.warn(msg, RuntimeWarning, stacklevel=3)
 
     def run(self, step0, nsteps, cache_tables=False):
-        """Advance the field by ``nsteps`` steps starting at global step ``step0``."""
+        """Advance the field by ``nsteps`` steps starting at global step ``step0``;
+        True when the potential came out non-finite (the caller reports it with
+        ``report_nonfinite`` once its step counter is advanced)."""
         if nsteps <= 0:
-            return
+            return False
         plan = self.prepare(step0, nsteps, cache_tables)
         self.launch(plan)
-        self.finish(plan)
+        return self.finish(plan)

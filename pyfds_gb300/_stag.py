@@ -82,7 +82,8 @@ class StagField:
         """Simulate one step (``self.step``; ``simulate`` advances the counter)."""
         if not self.matrices_assembled:
             self.assemble_matrices()
-        self._engine().run(self.step, 1, cache_tables=True)
+        if self._engine().run(self.step, 1, cache_tables=True):
+            self._engine().report_nonfinite(self.step + 1)
 
     _gpu_sim_step = sim_step
 

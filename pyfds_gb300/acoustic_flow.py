@@ -57,7 +57,8 @@ class AcousticFlow2D(Acoustic2D):
         (pyfds/acoustic_flow.py:44-47), in one library call."""
         if not self.matrices_assembled:
             self.assemble_matrices()
-        self._engine().run(self.step, 1, cache_tables=True)
+        if self._engine().run(self.step, 1, cache_tables=True):
+            self._engine().report_nonfinite(self.step + 1)
 
     _gpu_sim_step = sim_step
 

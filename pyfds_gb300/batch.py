@@ -114,14 +114,19 @@ class BatchRunner:
         self.graph.replay()
 
     def finish(self):
-        """Record outputs into ``Output.signals`` and advance every field's step."""
+        """Record outputs into ``Output.signals`` and advance every field's step; then
+        report the fields whose potential came out non-finite."""
+        diverged = []
         for f, plan in zip(self.fields, self.plans):
             eng = f._engine()
             for name in f._stag_components:
                 getattr(f, name)._where = "device"
             eng._last = plan
-            eng.finish(plan)
+            if eng.finish(plan):
+                diverged.append(f)
             f.step += self.num_steps
+        for f in diverged:
+            f._engine().report_nonfinite(f.step)
 
 
 def launch_count(num_steps, steps_per_launch):

@@ -78,8 +78,10 @@ class ThermoAcoustic1D(cp.SynchronizedFields):
             num_steps = self.t.samples
         if not self.matrices_assembled:
             self.assemble_matrices()
-        self._run_native(self.step, int(num_steps))
+        diverged = self._run_native(self.step, int(num_steps))
         self.step = self.step + int(num_steps)
+        for eng in diverged:
+            eng.report_nonfinite(self.step)
 
     def _run_native(self, step0, n):
         torch = require_cuda()
@@ -119,6 +121,7 @@ class ThermoAcoustic1D(cp.SynchronizedFields):
             int(self._loss.stepping), 1 if self._loss.accumulate else 0, int(step0), int(n),
             C.c_void_p(torch.cuda.current_stream().cuda_stream))
         _capi.check(code)
+        diverged = []
         for eng, f, st, plan in ((ea, acf, states[0], pa), (et, thf, states[1], pt)):
             for k, name in enumerate(f._stag_components):
                 bufs = eng.buffers[name]
@@ -126,6 +129,8 @@ class ThermoAcoustic1D(cp.SynchronizedFields):
                     bufs.reverse()
                 getattr(f, name)._where = "device"
             eng._last = plan
-            eng.finish(plan)
+            if eng.finish(plan):
+                diverged.append(eng)
         if self._loss.accumulate:
             self._loss.accumulated_transfer = 0 if empty.value else acc.cpu().numpy()
+        return diverged

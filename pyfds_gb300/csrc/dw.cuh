@@ -116,4 +116,15 @@ __device__ __forceinline__ dw ldg_t<dw>(const dw* p) {
   return dw(v.x, v.y);
 }
 
+// Load from L2 (not L1): state written by other CTAs of a running kernel.
+template <typename T>
+__device__ __forceinline__ T ldcg_t(const T* p) {
+  return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ dw ldcg_t<dw>(const dw* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return dw(v.x, v.y);
+}
+
 }  // namespace fds

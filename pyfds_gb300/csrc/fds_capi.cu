@@ -90,7 +90,7 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
   using namespace fds;
   if (!prob || !state || !tables) return set_error(FDS_E_ARG, "null argument");
   if (prob->nx < 1 || prob->ny < 1) return set_error(FDS_E_ARG, "bad grid %d x %d", prob->nx, prob->ny);
-  if (prob->stages < 0 || prob->stages > 3) return set_error(FDS_E_ARG, "bad stages %d", prob->stages);
+  if (prob->stages < 0 || prob->stages > 4) return set_error(FDS_E_ARG, "bad stages %d", prob->stages);
   if (nsteps < 0 || step0 < 0) return set_error(FDS_E_ARG, "bad step range");
   const bool has_v = (prob->flags & FDS_FLAG_HAS_V) != 0;
   if (!has_v && prob->ny != 1) return set_error(FDS_E_ARG, "1-D field needs ny == 1");
@@ -136,6 +136,14 @@ int32_t fds_stag_run(const FdsStagProblem* prob, FdsStagState* state,
     default:
       return set_error(FDS_E_ARG, "unknown precision %d", prob->precision);
   }
+}
+
+int64_t fds_stag_sync_words(const FdsStagProblem* prob) {
+  if (!prob) return fds::set_error(FDS_E_ARG, "null argument");
+  if (prob->nx < 1 || prob->ny < 1 || prob->tile_y < 1)
+    return fds::set_error(FDS_E_ARG, "bad grid %d x %d or tile height %d", prob->nx, prob->ny,
+                          prob->tile_y);
+  return 1 + ((int64_t)prob->ny + prob->tile_y - 1) / prob->tile_y;
 }
 
 size_t fds_stag_batch_workspace_bytes(int32_t count, int64_t total_tiles) {

@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(C::NT, 4)
   const int task = blockIdx.x * C::NW + (threadIdx.x >> 5);
   if (task >= a.ntiles) return;  // the whole warp leaves together
   const bool iso = a.iso != 0;
-  const int tx = task % a.tiles_x;
-  const int ty = task / a.tiles_x;
+  const int ty = tile_row(a, task);
+  const int tx = task - ty * a.tiles_x;
   const int c0 = tx * W;
   const int y0 = ty * TY;
   const int cend = min(c0 + W, a.nx);  // owned columns [c0, cend)

@@ -53,6 +53,8 @@ struct StagCore {
   int32_t nx, ny;
   int64_t n;
   int32_t tiles_x;
+  int32_t tx_shift;  // tile row = (tile * tx_mul) >> tx_shift (division by tiles_x)
+  uint64_t tx_mul;
   const TP* p_in;
   TP* p_out;
   const TF* u_in;
@@ -103,6 +105,33 @@ struct StepInfo {
 template <typename TP, typename TF, typename TC>
 __device__ __forceinline__ StepInfo step_of(const StagCore<TP, TF, TC>& a) {
   return StepInfo{a.step, a.step0, a.apply_next, a.store_flux, a.substeps};
+}
+
+// Tile row and column of a tile index without an integer division (which the
+// compiler builds from float conversions, per thread): the host sets tx_mul =
+// ceil(2^(32+l) / tiles_x) and tx_shift = 32 + l with l = ceil(log2(tiles_x)); for
+// tile < 2^31 the product stays below 2^64 and the quotient is exact (the rounding
+// error of tx_mul adds less than 1 / tiles_x to tile / tiles_x).
+template <typename TP, typename TF, typename TC>
+__device__ __forceinline__ int tile_row(const StagCore<TP, TF, TC>& a, int tile) {
+  return (int)(((uint64_t)(uint32_t)tile * a.tx_mul) >> a.tx_shift);
+}
+
+// Cell origin (x0, y0) of a tile.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ void tile_origin(const StagCore<TP, TF, TC>& a, int tile, int& x0,
+                                            int& y0) {
+  const int ty = tile_row(a, tile);
+  x0 = (tile - ty * a.tiles_x) * C::TX;
+  y0 = ty * C::TY;
+}
+
+// Host side of tile_row: the multiplier and shift for `tiles_x` columns of tiles.
+inline void tile_divider(int32_t tiles_x, uint64_t* mul, int32_t* shift) {
+  int l = 0;
+  while ((1ll << l) < (long long)tiles_x) ++l;
+  *shift = 32 + l;
+  *mul = ((1ull << (32 + l)) + (uint64_t)tiles_x - 1) / (uint64_t)tiles_x;
 }
 
 // Resident CTAs per SM the 256-thread 2-D tile kernels are compiled for (the
@@ -182,6 +211,16 @@ __device__ __forceinline__ dw xmul(const dw& a, const dw& b) { return a * b; }
 __device__ __forceinline__ dw xadd(const dw& a, const dw& b) { return a + b; }
 __device__ __forceinline__ dw xsub(const dw& a, const dw& b) { return a - b; }
 
+// NaN or infinity, from the exponent bits (integer instructions only: the FP64 pipe
+// stays free for the step's arithmetic).
+__device__ __forceinline__ bool nonfinite(double x) {
+  return ((__double2hiint(x) >> 20) & 0x7ff) == 0x7ff;
+}
+__device__ __forceinline__ bool nonfinite(float x) {
+  return ((__float_as_uint(x) >> 23) & 0xff) == 0xff;
+}
+__device__ __forceinline__ bool nonfinite(const dw& x) { return nonfinite(x.hi); }
+
 // Boundary chains of one component for this tile, applied to shared slots.
 // new = additive * old + value, additive as a number (pyfds/regions.py:125-145)
 template <int NT, typename T>
@@ -202,6 +241,12 @@ __device__ __forceinline__ void apply_bound_groups(const FdsCompTables& tb, int 
     }
     s[grp.pos] = v;
   }
+}
+
+// True if the tile has entries in a per-tile table (tile_start[tile] <
+// tile_start[tile + 1]); false for a missing table. The same for every thread.
+__device__ __forceinline__ bool tile_has(const int32_t* tile_start, int tile) {
+  return tile_start != nullptr && tile_start[tile] < tile_start[tile + 1];
 }
 
 template <int NT, typename T>
@@ -300,6 +345,33 @@ __device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* 
   }
 }
 
+// flux_new for the lossless, non-exact variants with the neighbour offset `back` as a
+// runtime value (1: x flux, RX: y flux); the same arithmetic as flux_new.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TF flux_lossless(const TP* sP, const TF* sF, const TC* sB, int pos,
+                                            int back, double offset) {
+  static_assert(!C::EXACT && !C::ABSORB, "lossless, non-exact variants only");
+  const TF b = (TF)sB[pos];
+  const TF bm = (TF)sB[pos - back];
+  const TF p = (TF)sP[pos];
+  const TF pm = (TF)sP[pos - back];
+  if constexpr (!C::MEMORY) {
+    if constexpr (sizeof(TP) > sizeof(TF)) {
+      const TP bp = (TP)sB[pos] * sP[pos];
+      return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
+    } else if constexpr (sizeof(TF) == 4 || std::is_same<TF, dw>::value) {
+      return settle(fma(-(b - bm), (TF)offset, fma(bm, pm, -(b * p))));
+    } else {
+      return settle(fma(bm, pm, -(b * p)));
+    }
+  } else {
+    TF acc = sF[pos];
+    acc = fma(-b, p, acc);
+    acc = fma(bm, pm, acc);
+    return settle(acc);
+  }
+}
+
 // Shared memory of one staging buffer of this variant; every array starts on a
 // 128-byte boundary (TMA destinations).
 __host__ __device__ constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
@@ -388,8 +460,8 @@ __device__ __forceinline__ void stage_tile(const StagCore<TP, TF, TC>& a, int ti
   const TC* kx = a.kx;
   const TC* by = a.by;
   const TC* ky = a.ky;
-  const int x0 = (tile % a.tiles_x) * C::TX;
-  const int y0 = (tile / a.tiles_x) * C::TY;
+  int x0, y0;
+  tile_origin<C>(a, tile, x0, y0);
   int c = threadIdx.x % RX;
   int64_t f = (int64_t)(y0 + (int)threadIdx.x / RX - OY) * nx + (x0 + c - C::OX);
   const int64_t df = (int64_t)DR * nx + DC;
@@ -423,8 +495,10 @@ __device__ __forceinline__ void tma_issue_tile(const StagCore<TP, TF, TC>& a, co
                                                int tile, const StagBuf<TP, TF, TC>& b, bool iso,
                                                uint64_t* bar) {
   constexpr int RN = C::RN;
-  const int gx = (tile % a.tiles_x) * C::TX - C::OX;
-  const int gy = (tile / a.tiles_x) * C::TY - C::OY;
+  int gx, gy;
+  tile_origin<C>(a, tile, gx, gy);
+  gx -= C::OX;
+  gy -= C::OY;
   uint32_t bytes = RN * (uint32_t)(sizeof(TP) + 2 * sizeof(TC));
   if constexpr (C::MEMORY) bytes += (C::HAS_V ? 2 : 1) * RN * (uint32_t)sizeof(TF);
   if (!iso) bytes += 2 * RN * (uint32_t)sizeof(TC);
@@ -450,8 +524,10 @@ __device__ __forceinline__ void tma_issue_tile(const StagCore<TP, TF, TC>& a, co
 template <class C, typename TP, typename TF, typename TC>
 __device__ __forceinline__ void tma_prefetch_tile(const StagCore<TP, TF, TC>& a,
                                                   const CUtensorMap* tm, int tile, bool iso) {
-  const int gx = (tile % a.tiles_x) * C::TX - C::OX;
-  const int gy = (tile / a.tiles_x) * C::TY - C::OY;
+  int gx, gy;
+  tile_origin<C>(a, tile, gx, gy);
+  gx -= C::OX;
+  gy -= C::OY;
   if (gx < 0 || gy < 0 || gx + C::RX > a.nx || gy + C::RY > a.ny) return;
   tma_prefetch_2d(&tm[0], gx, gy);
   if constexpr (C::MEMORY) {
@@ -475,8 +551,8 @@ __device__ __forceinline__ bool tma_finish_tile(const StagCore<TP, TF, TC>& a, i
                                                 uint64_t* bar, uint32_t parity) {
   constexpr int RX = C::RX, RN = C::RN, OX = C::OX, OY = C::OY, NT = C::NT;
   constexpr long long kWaitLimit = 1ll << 22;
-  const int x0 = (tile % a.tiles_x) * C::TX;
-  const int y0 = (tile / a.tiles_x) * C::TY;
+  int x0, y0;
+  tile_origin<C>(a, tile, x0, y0);
   bool ok = mbar_wait(bar, parity, kWaitLimit);
   if (__syncthreads_or(!ok)) {
     // give the copies in flight a second bounded chance to land before leaving
@@ -498,10 +574,12 @@ __device__ __forceinline__ bool tma_finish_tile(const StagCore<TP, TF, TC>& a, i
       const int x = x0 - OX + cc;
       const int64_t f = (int64_t)(y0 - OY + r) * a.nx + x;
       const bool in = (f >= 0 && f < a.n);
-      b.P[e] = in ? a.p_in[f] : TP(0);
+      // state through L2: in the persistent wavefront kernel other CTAs wrote it
+      // during this launch
+      b.P[e] = in ? ldcg_t(a.p_in + f) : TP(0);
       if constexpr (C::MEMORY) {
-        b.U[e] = in ? a.u_in[f] : TF(0);
-        if constexpr (C::HAS_V) b.V[e] = in ? a.v_in[f] : TF(0);
+        b.U[e] = in ? ldcg_t(a.u_in + f) : TF(0);
+        if constexpr (C::HAS_V) b.V[e] = in ? ldcg_t(a.v_in + f) : TF(0);
       }
       b.Bx[e] = in ? a.bx[f] : TC(0);
       b.Kx[e] = in ? a.kx[f] : TC(0);
@@ -538,8 +616,8 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   const TC* sKx = b.Kx;
   const TC* sBy = b.By;
   const TC* sKy = b.Ky;
-  const int x0 = (tile % a.tiles_x) * TX;
-  const int y0 = (tile / a.tiles_x) * TY;
+  int x0, y0;
+  tile_origin<C>(a, tile, x0, y0);
   const int x1 = min(x0 + TX, a.nx);  // end of owned columns
   const int y1 = min(y0 + TY, a.ny);
   const int tid = threadIdx.x;
@@ -583,10 +661,23 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   }
   TF uh = TF(0), vh = TF(0);
   const bool hu_ok = hu && (y0 + tid < y1) && hu_f < a.n;
-  if (hu_ok) uh = flux_new<C, true>(a, sP, sU, sBx, hu_pos, hu_f, x1 == a.nx ? 0 : x1);
   const bool hv_ok = hv && (x0 + hv_lx < x1) && hv_f < a.n;
-  if constexpr (C::HAS_V)
-    if (hv_ok) vh = flux_new<C, false>(a, sP, sV, sBy, hv_pos, hv_f, x0 + hv_lx);
+  if constexpr (C::HAS_V && !C::EXACT && !C::ABSORB) {
+    // both halo strips through one code path: the warp holding the U column and the
+    // start of the V row issues its flux arithmetic once, with every lane busy
+    // (the x and y flux differ only in the neighbour offset and the arrays)
+    const bool isx = tid < TY;
+    const TF h = (isx ? hu_ok : hv_ok)
+                     ? flux_lossless<C>(sP, isx ? sU : sV, isx ? sBx : sBy,
+                                        isx ? hu_pos : hv_pos, isx ? 1 : RX, a.offset)
+                     : TF(0);
+    uh = h;
+    vh = h;
+  } else {
+    if (hu_ok) uh = flux_new<C, true>(a, sP, sU, sBx, hu_pos, hu_f, x1 == a.nx ? 0 : x1);
+    if constexpr (C::HAS_V)
+      if (hv_ok) vh = flux_new<C, false>(a, sP, sV, sBy, hv_pos, hv_f, x0 + hv_lx);
+  }
   if constexpr (C::MEMORY && C::ABSORB) __syncthreads();  // neighbours read the old flux
 #pragma unroll
   for (int k = 0; k < OIT; ++k) {
@@ -599,9 +690,14 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   __syncthreads();
 
   // ---- flux bounds and probes (this step) ----
-  apply_bound_groups<NT>(a.tab[1], tile, sU, a.pool, si.step);
-  if constexpr (C::HAS_V) apply_bound_groups<NT>(a.tab[2], tile, sV, a.pool, si.step);
-  __syncthreads();
+  // (tiles without flux bounds, most of them, skip the barrier: the potential update
+  // and the probes read the fluxes as the barrier above left them)
+  if (tile_has(a.tab[1].bound_tile_start, tile) ||
+      (C::HAS_V && tile_has(a.tab[2].bound_tile_start, tile))) {
+    apply_bound_groups<NT>(a.tab[1], tile, sU, a.pool, si.step);
+    if constexpr (C::HAS_V) apply_bound_groups<NT>(a.tab[2], tile, sV, a.pool, si.step);
+    __syncthreads();
+  }
   write_probes<NT>(a.tab[1], tile, sU, si.step - si.step0);
   if constexpr (C::HAS_V) write_probes<NT>(a.tab[2], tile, sV, si.step - si.step0);
 
@@ -664,11 +760,15 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
       }
     }
   }
-  __syncthreads();  // all reads of sP done
+  // the next step's potential bounds and probes go through shared memory; a tile
+  // without them (most tiles) keeps the new potential in registers. No barrier is
+  // needed before the write: in the update above each thread read only the potential
+  // of its own cells.
+  if (si.apply_next && (tile_has(a.tab[0].bound_tile_start, tile) ||
+                        tile_has(a.tab[0].probe_tile_start, tile))) {
 #pragma unroll
-  for (int k = 0; k < OIT; ++k)
-    if (own[k]) sP[pos[k]] = pn[k];
-  if (si.apply_next) {
+    for (int k = 0; k < OIT; ++k)
+      if (own[k]) sP[pos[k]] = pn[k];
     __syncthreads();
     apply_bound_groups<NT>(a.tab[0], tile, sP, a.pool, si.step + 1);
     __syncthreads();
@@ -681,6 +781,14 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
 #pragma unroll
   for (int k = 0; k < OIT; ++k)
     if (own[k]) a.p_out[fo[k]] = pn[k];
+  // the last step of a call reports a diverged field (NaN and infinity spread, so
+  // the final potential shows any earlier blow-up)
+  if (!si.apply_next && a.status) {
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < OIT; ++k) bad = bad || (own[k] && nonfinite(pn[k]));
+    if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(a.status, kStatusNonFinite);
+  }
 }
 
 // Grid-stride over tiles. STAGES == 1: one tile per CTA, staged then computed.
@@ -755,6 +863,129 @@ __global__ void __launch_bounds__(C::NT, C::min_blocks(sizeof(TP), std::is_same<
   }
 }
 
+// ------------------------------------------------------- every step in one launch
+//
+// Persistent wavefront over a whole call (stages 4): each CTA takes work items
+// (step s, tile t) from a queue in the order item = s * ntiles + t, waits until the
+// tile rows around t finished step s - 1, stages its region with TMA, computes it
+// with compute_tile and publishes one more finished tile of its row. A tile's region
+// (rows y0 - 1 .. y0 + TY + 1, and through the flat-index wrap the neighbouring
+// rows' edge cells) lies in tile rows ty - 1 .. ty + 1 for TY >= 3, and those rows
+// also cover every tile that reads the cells this tile overwrites (ping-pong
+// buffers: step s writes what step s - 2 read). So the per-row counters order every
+// read after the write it needs and every overwrite after the reads of the old
+// values. Consecutive steps overlap and no launch boundary separates them: the
+// one-launch-per-step kernel spends about a tenth of each launch with SMs idle in
+// the wave tail and ramp.
+//
+// No deadlock: items are handed out in order, so the smallest unfinished item is
+// held by a running CTA and every item it waits for has a smaller index and is
+// finished. Every wait is bounded (status bit kStatusTmaTimeout, the CTA returns).
+template <typename TP, typename TF, typename TC>
+struct StagWaveArgs {
+  StagArgs<TP, TF, TC> par[2];  // step parity 0 reads the cur buffers, 1 the nxt ones
+  uint32_t* sync;    // [0]: next work item; [1 + r]: tiles of row r done, summed over steps
+  int32_t tiles_y;
+  int32_t nsteps;    // steps of this launch
+  int64_t step;      // global step of the launch's first step
+  int32_t flux_all;  // store the fluxes on every step (else on the call's last only)
+  int32_t more;      // steps of the same call follow this launch
+  int32_t prefetch;  // L2 prefetch distance in work items (0: off)
+};
+
+constexpr long long kWaveWaitLimit = 1ll << 22;
+
+// Thread 0: wait (bounded) until tile rows ty - 1 .. ty + 1 have finished `s` steps.
+template <typename TP, typename TF, typename TC>
+__device__ __forceinline__ bool wave_wait_rows(const StagWaveArgs<TP, TF, TC>& w, int ty, int s) {
+  const int r0 = ty > 0 ? ty - 1 : 0;
+  const int r1 = ty + 1 < w.tiles_y ? ty + 1 : w.tiles_y - 1;
+  if (!wait_counters(w.sync + 1, r0, r1, (uint32_t)s * (uint32_t)w.par[0].tiles_x,
+                     kWaveWaitLimit))
+    return false;
+  // the tensor copies (async proxy) read what other CTAs stored (generic proxy)
+  asm volatile("fence.proxy.async.global;\n" ::: "memory");
+  return true;
+}
+
+// Resident CTAs per SM the wavefront kernel is compiled for: the one-stage kernel's
+// figure, or fewer where its staging buffer fits fewer CTAs into the SM's 228 KB
+// (1 KB reserved per CTA), so that the register budget is not cut for CTAs that
+// could never be resident (float64 64 x 16: 4, 64 registers instead of 48 and
+// spills).
+template <class C, typename TP, typename TF, typename TC>
+__host__ __device__ constexpr int wave_blocks() {
+  constexpr int by_regs = C::min_blocks(sizeof(TP), std::is_same<TP, dw>::value);
+  constexpr int by_smem =
+      (int)((228u * 1024u) / (stag_buffer_bytes<C, TP, TF, TC>(true) + 16u + 1024u));
+  return by_smem < by_regs ? (by_smem > 0 ? by_smem : 1) : by_regs;
+}
+
+template <class C, typename TP, typename TF, typename TC>
+__global__ void __launch_bounds__(C::NT, (wave_blocks<C, TP, TF, TC>()))
+    stag_wave_kernel(const __grid_constant__ StagWaveArgs<TP, TF, TC> w) {
+  static_assert(C::STAGES == 1 && C::HAS_V && !C::TWO_STEP && C::TY >= 3,
+                "one-stage 2-D tiles at least three rows high");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ int s_item[2];
+  const bool iso = w.par[0].iso != 0;
+  const size_t bytes = stag_buffer_bytes<C, TP, TF, TC>(iso);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + bytes);
+  const StagBuf<TP, TF, TC> buf = carve_buffer<C, TP, TF, TC>(smem_raw, iso);
+  const int ntiles = w.par[0].ntiles;
+  const uint32_t total = (uint32_t)w.nsteps * (uint32_t)ntiles;
+  int32_t* status = w.par[0].status;
+  if (threadIdx.x == 0) mbar_init(bar, 1);
+  __syncthreads();
+  uint32_t uses = 0;  // completed phases of the mbarrier
+  // thread 0 takes each next item from the queue as soon as the current tile's copies
+  // are issued, so the atomic's round trip overlaps the copies and the compute
+  uint32_t next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(w.sync, 1u);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t item = next;
+      int s = -1, tile = 0;
+      if (item < total) {
+        s = (int)(item / (uint32_t)ntiles);
+        tile = (int)(item - (uint32_t)s * (uint32_t)ntiles);
+        const StagArgs<TP, TF, TC>& a = w.par[s & 1];
+        if (s > 0 && !wave_wait_rows(w, tile_row(a, tile), s)) {
+          if (status) atomicOr(status, kStatusTmaTimeout);
+          s = -2;
+        } else {
+          tma_issue_tile<C>(a, a.tm, tile, buf, iso, bar);
+          next = atomicAdd(w.sync, 1u);
+          const uint32_t ahead = item + (uint32_t)w.prefetch;
+          if (w.prefetch > 0 && ahead < total) {
+            const int s2 = (int)(ahead / (uint32_t)ntiles);
+            tma_prefetch_tile<C>(w.par[s2 & 1], w.par[s2 & 1].tm,
+                                 (int)(ahead - (uint32_t)s2 * (uint32_t)ntiles), iso);
+          }
+        }
+      }
+      s_item[0] = s;
+      s_item[1] = tile;
+    }
+    __syncthreads();
+    const int s = s_item[0], tile = s_item[1];
+    if (s < 0) break;  // queue empty, or a wait gave up (nothing in flight)
+    const StagArgs<TP, TF, TC>& a = w.par[s & 1];
+    if (!tma_finish_tile<C>(a, tile, buf, iso, bar, uses & 1u)) return;
+    ++uses;
+    const bool last = s + 1 == w.nsteps;
+    compute_tile<C>(a,
+                    StepInfo{w.step + s, a.step0, (!last || w.more) ? 1 : 0,
+                             (w.flux_all || (last && !w.more)) ? 1 : 0, 1},
+                    tile, buf);
+    __syncthreads();  // every thread's stores are issued and the buffer is free
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(w.sync + 1 + tile_row(a, tile), 1u);
+    }
+  }
+}
+
 // ------------------------------------------------------------ two steps per tile
 //
 // Temporal blocking for the lossless 2-D variants (memory-bound precisions): a
@@ -820,8 +1051,8 @@ template <class C, typename TP, typename TF, typename TC>
 __device__ __forceinline__ void compute_ring(const StagCore<TP, TF, TC>& a, const StepInfo si,
                                              int tile, const StagBuf<TP, TF, TC>& b) {
   constexpr int TX = C::TX, TY = C::TY, NT = C::NT, RX = C::RX, OX = C::OX, OY = C::OY;
-  const int x0 = (tile % a.tiles_x) * TX;
-  const int y0 = (tile / a.tiles_x) * TY;
+  int x0, y0;
+  tile_origin<C>(a, tile, x0, y0);
   // fluxes: each slot reads only its own old flux and the potential. Slots of
   // cells outside the field get 0, as in the one-step kernel (thermal fluxes are
   // not staged, so those slots would otherwise hold stale shared memory, which the

@@ -13,6 +13,7 @@ namespace fds {
 
 // Status bits a kernel ORs into FdsStagTables.status.
 constexpr int32_t kStatusTmaTimeout = 1;
+constexpr int32_t kStatusNonFinite = 2;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -66,6 +67,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
     if (done) return true;
   }
   return false;
+}
+
+// Waits until counters c[r0 .. r1] (global memory, written by other CTAs) have each
+// reached `need`, reading them with acquire semantics; gives up after `limit` polls
+// of one counter (a short sleep between polls).
+__device__ __forceinline__ bool wait_counters(const uint32_t* c, int r0, int r1, uint32_t need,
+                                              long long limit) {
+  for (int r = r0; r <= r1; ++r) {
+    long long i = 0;
+    for (;;) {
+      uint32_t v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(c + r) : "memory");
+      if (v >= need) break;
+      if (++i > limit) return false;
+      __nanosleep(64);
+    }
+  }
+  return true;
 }
 
 // ---------------------------------------------------------------- host side

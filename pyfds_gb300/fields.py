@@ -84,10 +84,12 @@ class Field:
                 edges = sorted({int(round(num_steps * k / 20)) for k in range(21)})
                 chunks = [b - a for a, b in zip(edges[:-1], edges[1:]) if b > a]
             for n in chunks:
-                self._engine().run(self.step, n)
+                diverged = self._engine().run(self.step, n)
                 if progress_logger:
                     progress_logger.log(self.step + n - 1)
                 self.step += n
+                if diverged:
+                    self._engine().report_nonfinite(self.step)
         else:
             while self.step < start_step + num_steps:
                 self.sim_step()

@@ -51,6 +51,17 @@ DEFAULT_LAYERS = ((16, 48, 1, "first"), (48, 48, 2, "res"), (48, 48, 4, "res"),
                   (48, 48, 2, "res"), (48, 16, 1, "out"))
 
 
+def initial_weights(layers, seed):
+    """Seeded initial weights [(w [9][cout][cin], b [cout]), ...]: He-scaled normal
+    draws, shrunk on the residual (0.2) and output (0.05) layers, zero biases."""
+    rng = np.random.default_rng(seed)
+    ws = []
+    for cin, cout, dil, kind in layers:
+        std = math.sqrt(2.0 / (9 * cin)) * {"first": 1.0, "res": 0.2, "out": 0.05}[kind]
+        ws.append((rng.standard_normal((9, cout, cin)) * std, np.zeros(cout)))
+    return ws
+
+
 def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
@@ -76,13 +87,8 @@ class ConvNet:
         if self.layers[0][0] != IN_CH or self.layers[-1][1] != OUT_CH:
             raise ValueError("the first layer takes %d channels, the last gives %d"
                              % (IN_CH, OUT_CH))
-        rng = np.random.default_rng(seed)
-        ws = []
-        for cin, cout, dil, kind in self.layers:
-            std = math.sqrt(2.0 / (9 * cin)) * {"first": 1.0, "res": 0.2, "out": 0.05}[kind]
-            ws.append((rng.standard_normal((9, cout, cin)) * std, np.zeros(cout)))
         self.params = [None] * len(self.layers)
-        self.set_weights(ws)
+        self.set_weights(initial_weights(self.layers, seed))
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.step_count = 0
         self.grid = int(self.lib.fds_conv_wgrad_max_grid())
@@ -301,13 +307,14 @@ def _fd_runner(fields, warmup=True):
     return r
 
 
-def generate_data(count, nsnap, seed, n=256):
+def generate_data(count, nsnap, seed, n=256, jump=JUMP):
     """Snapshots from the batched FP64 solver: ``count`` media (surrogate_media),
-    ``T_SRC`` solver steps through the source pulse, then ``nsnap`` snapshots 64
-    steps apart (state copied on the device, float32)."""
+    ``T_SRC`` solver steps through the source pulse, then ``nsnap`` snapshots
+    ``jump`` steps apart (64, the network's jump; state copied on the device,
+    float32)."""
     torch = require_cuda()
     dev = torch.device("cuda", torch.cuda.current_device())
-    specs = workloads.surrogate_media(count, seed, n=n, nt=T_SRC + nsnap * JUMP + JUMP)
+    specs = workloads.surrogate_media(count, seed, n=n, nt=T_SRC + nsnap * jump + jump)
     fields = [workloads.build_field(s) for s in specs]
     simulate_batch(fields, T_SRC)
     state = torch.empty((count, nsnap, 3, n, n), dtype=torch.float32, device=dev)
@@ -319,7 +326,7 @@ def generate_data(count, nsnap, seed, n=256):
                 state[i, k, c].copy_(eng.buffers[nm][0].view(n, n))
 
     snap(0)
-    r = BatchRunner(fields, JUMP)
+    r = BatchRunner(fields, jump)
     r.capture()  # the warm-up launch is the first jump
     for k in range(1, nsnap):
         if k > 1:
@@ -424,6 +431,22 @@ def rel_l2(net, a, b, zref, inst):
                                          _ptr(zref), _ptr(out), _stream(torch)))
     o = out.cpu().numpy().reshape(-1, 2)
     return np.sqrt(o[:, 0] / np.maximum(o[:, 1], 1e-300))
+
+
+def evaluate_jumps(net, data, jumps, chunk=64):
+    """Relative L2 error (rel_l2) of each instance of ``data`` after 1 .. ``jumps``
+    chained network jumps from its snapshot 0, against the solver's snapshots:
+    array [instances][jumps]."""
+    torch = net.torch
+    S = data.state[:, 0].to(torch.float64).contiguous()
+    inst = torch.arange(data.count, dtype=torch.int32, device=net.dev)
+    errs = []
+    for j in range(jumps):
+        jump(net, S, data.media, data.freq, data.zref, inst, chunk)
+        ref = data.state[:, j + 1].to(torch.float64).contiguous()
+        errs.append(rel_l2(net, S, ref, data.zref, inst))
+    net.check_status()
+    return np.stack(errs, axis=1)
 
 
 def _alias_state(fields, n, torch, dev):

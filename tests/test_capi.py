@@ -45,7 +45,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_capi.FdsStagProblem) == 8 * 4 + 11 * 8 + 8 + 8
     assert C.sizeof(_capi.FdsStagState) == 6 * 8
     assert C.sizeof(_capi.FdsCompTables) == 6 * 8 + 8
-    assert C.sizeof(_capi.FdsStagTables) == 3 * 56 + 24
+    assert C.sizeof(_capi.FdsStagTables) == 3 * 56 + 40
     assert _capi.BOUND_OP_DTYPE.itemsize == 32
     assert _capi.BOUND_GROUP_DTYPE.itemsize == 24
     assert _capi.PROBE_DTYPE.itemsize == 16
@@ -80,3 +80,26 @@ def test_argument_errors_are_reported(lib):
     assert "coefficient" in _capi.last_error()
     with pytest.raises(_capi.FdsError):
         _capi.check(_capi.FDS_E_ARG)
+
+
+def test_wavefront_scratch_size_and_checks(lib):
+    pr = _capi.FdsStagProblem()
+    pr.nx, pr.ny, pr.tile_x, pr.tile_y = 2048, 2048, 64, 16
+    assert lib.fds_stag_sync_words(C.byref(pr)) == 1 + 128
+    pr.ny = 17
+    assert lib.fds_stag_sync_words(C.byref(pr)) == 1 + 2
+    pr.ny = 0
+    assert lib.fds_stag_sync_words(C.byref(pr)) == _capi.FDS_E_ARG
+    assert lib.fds_stag_sync_words(None) == _capi.FDS_E_ARG
+    # stages beyond 4 are rejected before any GPU work
+    st, tb = _capi.FdsStagState(), _capi.FdsStagTables()
+    pr.ny, pr.stages = 16, 5
+    assert lib.fds_stag_run(C.byref(pr), C.byref(st), C.byref(tb), 0, 1, 1, None) == _capi.FDS_E_ARG
+    assert "stages" in _capi.last_error()
+
+
+def test_selftest_argument_checks(lib):
+    assert lib.fds_selftest_bounded_wait(2, None, None, 10, None) == _capi.FDS_E_ARG
+    assert lib.fds_selftest_bounded_wait(0, None, None, 10, None) == _capi.FDS_E_ARG
+    assert lib.fds_selftest_bounded_wait(0, C.c_void_p(256), None, 0, None) == _capi.FDS_E_ARG
+    assert lib.fds_selftest_bounded_wait(1, C.c_void_p(256), None, 10, None) == _capi.FDS_E_ARG

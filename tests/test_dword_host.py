@@ -98,8 +98,12 @@ def test_potential_offset_policy(precision, explicit, expected):
     ("Acoustic2D", "dw", {}, 0, False, 3),        # double-word acoustic: two steps
     ("Thermal2D", "dw", {}, 0, False, 0),         # double-word thermal keeps one
     ("Thermal2D", "f32", {}, 0, False, 3),
-    ("Acoustic2D", "f64", {}, 0, False, 0),       # float64 (FP64-bound) keeps one
+    ("Acoustic2D", "f64", {}, 0, False, 4),       # float64 acoustic: the wavefront run
+    ("Acoustic3DAxi", "f64", {}, 0, False, 4),    # (lossless axisymmetric steps as planar)
+    ("Thermal2D", "f64", {}, 0, False, 0),        # float64 thermal keeps one per launch
+    ("Acoustic2D", "f64", {"tile": (32, 32)}, 0, False, 0),  # no wavefront kernel
     ("Acoustic2D", "f64", {"exact": True}, 0, False, 0),
+    ("Acoustic2D", "f64", {}, 4, True, 3),        # batches have no wavefront run
     ("Acoustic2D", "f32", {}, 1, False, 1),       # an explicit choice stands
     ("Acoustic2D", "f64", {}, 3, False, 3),
     ("Acoustic2D", "f64", {}, 0, True, 3),        # batches: two steps for every precision
@@ -108,9 +112,9 @@ def test_potential_offset_policy(precision, explicit, expected):
     ("Acoustic1D", "f32", {}, 0, False, 0),       # 1-D: no two-step kernel
 ])
 def test_automatic_stages(kind, precision, kwargs, stages, batched, expected):
-    """StagEngine.stages: the field's choice when set; otherwise two steps per tile
-    where it was measured faster and a two-step kernel exists (lossless 2-D, not
-    exact, no moving medium, a two-step tile)."""
+    """StagEngine.stages: the field's choice when set; otherwise the wavefront run or
+    two steps per tile where measured faster and the kernel exists (lossless 2-D,
+    not exact, no moving medium, a tile with that kernel)."""
     from pyfds_gb300._engine import StagEngine
     spec = S.random_scenario(6, kind, 40, None if kind.endswith("1D") else 20, steps=2,
                              mu=False)

@@ -69,3 +69,34 @@ def test_surrogate_struct_layouts():
     assert C.sizeof(_capi.FdsWgradArgs) == 6 * 4 + 3 * 8 + 2 * 4 + 8
     assert C.sizeof(_capi.FdsAdamArgs) == 4 * 4 + 6 * 4 + 8 * 8
     assert C.sizeof(_capi.FdsSurrData) == 6 * 4 + 10 * 8
+
+
+def test_float32_twin_matches_the_oracle_network():
+    """The float32 twin of the precision study (pyfds_gb300.surrogate_twin) computes
+    the oracle's network (tap convention, dilations, GELU, residuals) on the same
+    initial weights, within float32 rounding."""
+    import torch
+    from pyfds_gb300 import surrogate as S
+    from pyfds_gb300 import surrogate_twin as T
+    tw = T.TwinNet(seed=3, device="cpu")
+    ws = S.initial_weights(S.DEFAULT_LAYERS, 3)
+    # larger biases and output weights than the initial ones exercise every term
+    rng = np.random.default_rng(5)
+    ws = [(w * (20.0 if k == len(ws) - 1 else 1.0), rng.standard_normal(b.shape) * 0.1)
+          for k, (w, b) in enumerate(ws)]
+    with torch.no_grad():
+        for conv, (w, b) in zip(tw.convs, ws):
+            cout, cin = w.shape[1], w.shape[2]
+            conv.weight.copy_(torch.tensor(np.asarray(w, dtype=np.float32).reshape(
+                3, 3, cout, cin).transpose(2, 3, 0, 1).copy()))
+            conv.bias.copy_(torch.tensor(np.asarray(b, dtype=np.float32)))
+    x = rng.standard_normal((2, 24, 20, 16))
+    params = [(torch.tensor(np.asarray(w, dtype=np.float32).astype(np.float64)),
+               torch.tensor(np.asarray(b, dtype=np.float32).astype(np.float64)))
+              for w, b in ws]
+    y_o, _ = so.forward(torch.tensor(x), params, S.DEFAULT_LAYERS, bf16=False)
+    with torch.no_grad():
+        y_t = tw.forward(torch.tensor(x, dtype=torch.float32).permute(0, 3, 1, 2))
+    y_t = y_t.permute(0, 2, 3, 1).double().numpy()
+    err = np.linalg.norm(y_t - y_o.numpy()) / np.linalg.norm(y_o.numpy())
+    assert err < 1e-5, err
