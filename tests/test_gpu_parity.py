@@ -139,6 +139,26 @@ def test_full_size_prefix_vs_reference(gpu, name, builder, comps):
     check_signals(sig, g, "", comps, exact=False)
 
 
+@pytest.mark.parametrize("name,builder,comps,stages", [
+    ("axi_disc_full_1000.npz", workloads.axi_disc_source, ["pressure"], 0),
+    ("axi_disc_full_1000.npz", workloads.axi_disc_source, ["pressure"], 1),
+    ("thermal2d_4096_1000.npz", workloads.thermal2d_two_materials, ["temperature"], 0),
+])
+def test_full_size_1000_steps_vs_reference(gpu, name, builder, comps, stages):
+    """The full-size axisymmetric (1024 x 4096, 64 outputs) and thermal (4096^2, 64
+    outputs) workloads for their first 1000 steps against the unmodified reference
+    (pyfds/acoustics.py:205-225, pyfds/thermal.py:92-107), every output at the 1e-12
+    bar: the automatic path (the wavefront run for the axisymmetric field) and one
+    launch per step."""
+    g = golden(name)
+    spec = apply_inputs(builder(), g)
+    f = build_field(spec)
+    f.stages = stages
+    f.simulate(1000)
+    st, sig = field_results(f)
+    assert check_signals(sig, g, "", comps, exact=False) <= TOL
+
+
 def test_sim_step_loop_equals_simulate(gpu):
     spec = S.random_scenario(7, "Acoustic2D", 70, 40, steps=12)
     a = build_field(spec)
