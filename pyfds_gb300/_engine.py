@@ -9,6 +9,7 @@ tensors; libfdsgpu.so only borrows the pointers.
 """
 import ctypes as C
 import warnings
+import zlib
 
 import numpy as np
 
@@ -111,6 +112,65 @@ class _Blob:
         return dev
 
 
+_PINNED = {"buf": None, "event": None}
+
+
+class HostUpload:
+    """Host arrays bound for many device tensors, sent in one copy.
+
+    ``add`` records (host array, destination tensor); ``flush`` packs the arrays into
+    one pinned staging buffer (kept between calls, grown on demand), copies it to the
+    device in one transfer and then fills every destination on the device: a copy
+    with the dtype conversion the destination asks for, or for double words the
+    split of float64 values into float32 pairs (fds_dw_split). A batch of fields
+    thus pays one host-to-device transfer instead of a few per field."""
+
+    def __init__(self, torch, device):
+        self.torch, self.device = torch, device
+        self.items = []
+        self.size = 0
+
+    def add(self, host, dst, dword=False):
+        b = np.ascontiguousarray(host)
+        off = self.size
+        self.items.append((off, b, dst, dword))
+        self.size = (off + b.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
+        return dst
+
+    def flush(self):
+        torch = self.torch
+        if not self.items:
+            return
+        ev = _PINNED["event"]
+        if ev is not None:
+            ev.synchronize()  # the previous flush's copy has left the pinned buffer
+        buf = _PINNED["buf"]
+        if buf is None or buf.numel() < self.size:
+            buf = torch.empty(max(self.size, 1 << 20), dtype=torch.uint8, pin_memory=True)
+            _PINNED["buf"] = buf
+        host = buf.numpy()
+        for off, b, _, _ in self.items:
+            host[off:off + b.nbytes] = b.view(np.uint8).reshape(-1)
+        staged = torch.empty(self.size, dtype=torch.uint8, device=self.device)
+        staged.copy_(buf[:self.size], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream())
+        _PINNED["event"] = ev
+        lib = _capi.load()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        dtypes = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+                  np.dtype(np.uint8): torch.uint8}
+        for off, b, dst, dword in self.items:
+            src = staged[off:off + b.nbytes]
+            if dword:
+                _capi.check(lib.fds_dw_split(C.c_void_p(src.data_ptr()),
+                                             C.c_void_p(dst.data_ptr()), b.size, stream))
+            else:
+                dst.view(-1).copy_(src.view(dtypes[b.dtype]))  # converts to dst's dtype
+        self.items = []
+        self.size = 0
+
+
 class StagEngine:
     """GPU state, coefficients and tables of one staggered field."""
 
@@ -136,7 +196,7 @@ class StagEngine:
         return torch.float64, torch.float32, torch.float32  # f32_t64: potential in float64
 
     # ------------------------------------------------------------ coefficients
-    def _upload_coefs(self, torch, dev):
+    def _upload_coefs(self, torch, dev, up=None):
         key = self.field._coef_version
         if key == self.coef_key:
             return
@@ -145,11 +205,17 @@ class StagEngine:
         for name, arr in self.field._stag_coefs.items():
             if arr is None:
                 continue
+            vals = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+            if up is not None:
+                dword = self.field.precision == "dw"
+                dst = torch.empty((vals.size, 2) if dword else (vals.size,),
+                                  dtype=torch.float32 if dword else tc, device=dev)
+                self.coef_tensors[name] = up.add(vals, dst, dword)
+                continue
             if self.field.precision == "dw":
                 self.coef_tensors[name] = upload_dw(torch, dev, arr)
                 continue
-            self.coef_tensors[name] = torch.from_numpy(
-                np.ascontiguousarray(arr, dtype=np.float64)).to(dev).to(tc)
+            self.coef_tensors[name] = torch.from_numpy(vals).to(dev).to(tc)
         self.coef_key = key
 
     def _flow_periods(self, torch, dev):
@@ -198,7 +264,7 @@ class StagEngine:
             self.offset = float(off)
         return self.offset
 
-    def _sync_state_to_device(self, torch, dev):
+    def _sync_state_to_device(self, torch, dev, up=None):
         tp, tf, _ = self.dtypes()
         names = self.field._stag_components
         off = self._potential_offset()
@@ -223,7 +289,9 @@ class StagEngine:
                                      % (name, vals.size, n))
                 if k == 0 and off:
                     vals = vals - off
-                if dword:
+                if up is not None:
+                    up.add(vals, bufs[0], dword)
+                elif dword:
                     upload_dw(torch, dev, vals, out=bufs[0])
                 else:
                     bufs[0].copy_(torch.from_numpy(np.ascontiguousarray(vals)).to(dev).to(dt))
@@ -318,20 +386,33 @@ class StagEngine:
                                     layout)
 
     def _fingerprint(self):
+        """What the tables are compiled from: the boundaries (objects, index lists and
+        values, with checksums of their contents so that in-place edits count) and the
+        outputs' index lists."""
+        def crc(a):
+            return zlib.crc32(np.ascontiguousarray(a).view(np.uint8).reshape(-1))
+
         parts = []
         for name in self.field._stag_components:
             comp = getattr(self.field, name)
             bp = []
             for b in comp.boundaries:
                 v = b.value
-                bp.append((id(b), id(b.region), id(b.region.indices), id(v),
-                           float(v) if np.ndim(v) == 0 else np.shape(v) if
-                           isinstance(v, np.ndarray) else len(v), b.additive))
-            op = tuple((id(o), id(o.region), id(o.region.indices)) for o in comp.outputs)
+                if np.ndim(v) == 0:
+                    vk = float(v)
+                elif isinstance(v, np.ndarray):
+                    vk = (np.shape(v), str(v.dtype), crc(v))
+                else:
+                    vk = (len(v), tuple(crc(np.asarray(x, dtype=np.float64)) for x in v))
+                idx = np.asarray(b.region.indices)
+                bp.append((id(b), id(b.region), id(b.region.indices), crc(idx), id(v), vk,
+                           b.additive))
+            op = tuple((id(o), id(o.region), id(o.region.indices),
+                        crc(np.asarray(o.region.indices))) for o in comp.outputs)
             parts.append((tuple(bp), op))
         return tuple(parts)
 
-    def _compile_tables(self, torch, dev, step_end, geo):
+    def _compile_tables(self, torch, dev, step_end, geo, up=None):
         f = self.field
         n = f.num_points
         pool = _tables.SignalPool()
@@ -356,7 +437,13 @@ class StagEngine:
             offs.append(o)
         pool_arr = pool.array()
         pool_off = blob.add(pool_arr)
-        dev_blob = blob.upload(torch, dev)
+        if up is not None:
+            host = np.zeros(max(blob.size, _ALIGN), dtype=np.uint8)
+            for off, b in blob.parts:
+                host[off:off + b.size] = b
+            dev_blob = up.add(host, torch.empty(host.size, dtype=torch.uint8, device=dev))
+        else:
+            dev_blob = blob.upload(torch, dev)
         return {"blob": dev_blob, "offs": offs, "ncols": [c[2] for c in comps],
                 "pool_off": pool_off, "pool_len": int(pool_arr.size)}
 
@@ -382,14 +469,16 @@ class StagEngine:
         return st
 
     # --------------------------------------------------------------------- run
-    def prepare(self, step0, nsteps, cache_tables=False, batched=False):
+    def prepare(self, step0, nsteps, cache_tables=False, batched=False, up=None):
         """Upload what the host changed and compile the tables for steps
-        ``step0 .. step0+nsteps-1``; returns a launch plan for ``launch``."""
+        ``step0 .. step0+nsteps-1``; returns a launch plan for ``launch``. With a
+        HostUpload ``up`` the host arrays go to the device when the caller flushes
+        it (before launching)."""
         torch = require_cuda()
         f = self.field
         dev = torch.device("cuda", torch.cuda.current_device())
-        self._upload_coefs(torch, dev)
-        self._sync_state_to_device(torch, dev)
+        self._upload_coefs(torch, dev, up)
+        self._sync_state_to_device(torch, dev, up)
         geo = self._geometry(batched)
         step_end = step0 + nsteps
         if cache_tables:
@@ -399,10 +488,10 @@ class StagEngine:
                     self.table_cache[2] >= step_end:
                 tabs = self.table_cache[1]
             else:
-                tabs = self._compile_tables(torch, dev, max(step_end, 1), geo)
+                tabs = self._compile_tables(torch, dev, max(step_end, 1), geo, up)
                 self.table_cache = (fp, tabs, step_end)
         else:
-            tabs = self._compile_tables(torch, dev, step_end, geo)
+            tabs = self._compile_tables(torch, dev, step_end, geo, up)
         outs = [torch.empty((nsteps, max(nc, 1)), dtype=torch.float64, device=dev)
                 if nc else None for nc in tabs["ncols"]]
         prob = _capi.FdsStagProblem()
@@ -462,12 +551,15 @@ class StagEngine:
             getattr(f, name)._where = "device"
         self._last = plan  # keeps the tables and output buffers alive
 
-    def finish(self, plan):
+    def finish(self, plan, status=None, host_outs=None):
         """Copy the output buffers to the host and append them to Output.signals;
         raise if a kernel reported a failed bounded wait. Returns True when the
-        kernels reported a non-finite potential (see ``report_nonfinite``)."""
+        kernels reported a non-finite potential (see ``report_nonfinite``).
+        ``status`` / ``host_outs``: the status word and the outputs (one host array
+        per component, None where it has no outputs) when the caller already copied
+        them to the host, as a batch does for all its fields at once."""
         f = self.field
-        st = int(self.status.item())
+        st = int(self.status.item()) if status is None else int(status)
         if st:
             self.status.zero_()
         if st & _capi.STATUS_TMA_TIMEOUT:
@@ -479,7 +571,7 @@ class StagEngine:
             out_t = plan["outs"][k]
             if out_t is None:
                 continue
-            host = out_t.to("cpu").numpy()
+            host = out_t.to("cpu").numpy() if host_outs is None else host_outs[k]
             if k == 0 and self.offset:
                 host = host + self.offset
             comp = getattr(f, name)

@@ -13,8 +13,9 @@ graph and replayed (parameter sweeps that reset and rerun the same set of fields
 """
 import ctypes as C
 
+
 from . import _capi
-from ._engine import require_cuda
+from ._engine import HostUpload, require_cuda
 
 
 class BatchRunner:
@@ -42,8 +43,14 @@ class BatchRunner:
             if not f.matrices_assembled:
                 f.assemble_matrices()
         self.step0 = int(f0.step)
-        self.plans = [f._engine().prepare(self.step0, self.num_steps, batched=True)
+        # every instance's coefficients, state and tables in one host-to-device copy;
+        # tables are reused while an instance's boundaries and outputs are unchanged
+        dev = self.torch.device("cuda", self.torch.cuda.current_device())
+        up = HostUpload(self.torch, dev)
+        self.plans = [f._engine().prepare(self.step0, self.num_steps, cache_tables=True,
+                                          batched=True, up=up)
                       for f in self.fields]
+        up.flush()
         n = len(self.fields)
         self.probs = (_capi.FdsStagProblem * n)(*[p["prob"] for p in self.plans])
         self.tables = (_capi.FdsStagTables * n)(*[p["tstruct"] for p in self.plans])
@@ -51,7 +58,6 @@ class BatchRunner:
         self.total_tiles = sum(p["geo"].ntiles for p in self.plans)
         lib = _capi.load()
         nbytes = lib.fds_stag_batch_workspace_bytes(n, self.total_tiles)
-        dev = self.torch.device("cuda", self.torch.cuda.current_device())
         self.workspace = self.torch.empty(nbytes, dtype=self.torch.uint8, device=dev)
         self._fill_states()
         self._call(_capi.BATCH_UPLOAD)
@@ -115,14 +121,27 @@ class BatchRunner:
 
     def finish(self):
         """Record outputs into ``Output.signals`` and advance every field's step; then
-        report the fields whose potential came out non-finite."""
+        report the fields whose potential came out non-finite. The status words and
+        outputs of all instances come to the host in one copy each."""
+        torch = self.torch
+        engs = [f._engine() for f in self.fields]
+        status = torch.cat([e.status for e in engs]).cpu().numpy()
+        outs = [o for p in self.plans for o in p["outs"] if o is not None]
+        flat = torch.cat([o.reshape(-1) for o in outs]).cpu().numpy() if outs else None
+        pos = 0
         diverged = []
-        for f, plan in zip(self.fields, self.plans):
-            eng = f._engine()
+        for f, eng, plan, st in zip(self.fields, engs, self.plans, status):
+            host_outs = []
+            for o in plan["outs"]:
+                if o is None:
+                    host_outs.append(None)
+                else:
+                    host_outs.append(flat[pos:pos + o.numel()].reshape(tuple(o.shape)))
+                    pos += o.numel()
             for name in f._stag_components:
                 getattr(f, name)._where = "device"
             eng._last = plan
-            if eng.finish(plan):
+            if eng.finish(plan, status=st, host_outs=host_outs):
                 diverged.append(f)
             f.step += self.num_steps
         for f in diverged:

@@ -895,17 +895,28 @@ struct StagWaveArgs {
 
 constexpr long long kWaveWaitLimit = 1ll << 22;
 
+// True if tile rows ty - 1 .. ty + 1 have finished `s` steps (one acquire load each).
+template <typename TP, typename TF, typename TC>
+__device__ __forceinline__ bool wave_rows_ready(const StagWaveArgs<TP, TF, TC>& w, int ty, int s) {
+  const uint32_t need = (uint32_t)s * (uint32_t)w.par[0].tiles_x;
+  const int r0 = ty > 0 ? ty - 1 : 0;
+  const int r1 = ty + 1 < w.tiles_y ? ty + 1 : w.tiles_y - 1;
+  bool ok = true;
+  for (int r = r0; r <= r1; ++r) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(w.sync + 1 + r) : "memory");
+    ok = ok && v >= need;
+  }
+  return ok;
+}
+
 // Thread 0: wait (bounded) until tile rows ty - 1 .. ty + 1 have finished `s` steps.
 template <typename TP, typename TF, typename TC>
 __device__ __forceinline__ bool wave_wait_rows(const StagWaveArgs<TP, TF, TC>& w, int ty, int s) {
   const int r0 = ty > 0 ? ty - 1 : 0;
   const int r1 = ty + 1 < w.tiles_y ? ty + 1 : w.tiles_y - 1;
-  if (!wait_counters(w.sync + 1, r0, r1, (uint32_t)s * (uint32_t)w.par[0].tiles_x,
-                     kWaveWaitLimit))
-    return false;
-  // the tensor copies (async proxy) read what other CTAs stored (generic proxy)
-  asm volatile("fence.proxy.async.global;\n" ::: "memory");
-  return true;
+  return wait_counters(w.sync + 1, r0, r1, (uint32_t)s * (uint32_t)w.par[0].tiles_x,
+                       kWaveWaitLimit);
 }
 
 // Resident CTAs per SM the wavefront kernel is compiled for: the one-stage kernel's
@@ -938,9 +949,12 @@ __global__ void __launch_bounds__(C::NT, (wave_blocks<C, TP, TF, TC>()))
   if (threadIdx.x == 0) mbar_init(bar, 1);
   __syncthreads();
   uint32_t uses = 0;  // completed phases of the mbarrier
-  // thread 0 takes each next item from the queue as soon as the current tile's copies
-  // are issued, so the atomic's round trip overlaps the copies and the compute
+  // Thread 0 takes each next item from the queue as soon as the current tile's copies
+  // are issued and checks its dependencies right away (the loads' round trips
+  // overlap the copies and the compute); only an item whose rows were not ready then
+  // is checked again, with the bounded wait, when its turn comes.
   uint32_t next = 0;
+  bool next_ready = false;
   if (threadIdx.x == 0) next = atomicAdd(w.sync, 1u);
   for (;;) {
     if (threadIdx.x == 0) {
@@ -950,12 +964,20 @@ __global__ void __launch_bounds__(C::NT, (wave_blocks<C, TP, TF, TC>()))
         s = (int)(item / (uint32_t)ntiles);
         tile = (int)(item - (uint32_t)s * (uint32_t)ntiles);
         const StagArgs<TP, TF, TC>& a = w.par[s & 1];
-        if (s > 0 && !wave_wait_rows(w, tile_row(a, tile), s)) {
+        if (s > 0 && !next_ready && !wave_wait_rows(w, tile_row(a, tile), s)) {
           if (status) atomicOr(status, kStatusTmaTimeout);
           s = -2;
         } else {
+          // the tensor copies (async proxy) read what other CTAs stored (generic proxy)
+          asm volatile("fence.proxy.async.global;\n" ::: "memory");
           tma_issue_tile<C>(a, a.tm, tile, buf, iso, bar);
           next = atomicAdd(w.sync, 1u);
+          next_ready = false;
+          if (next < total) {
+            const int s1 = (int)(next / (uint32_t)ntiles);
+            const int t1 = (int)(next - (uint32_t)s1 * (uint32_t)ntiles);
+            next_ready = s1 == 0 || wave_rows_ready(w, tile_row(w.par[0], t1), s1);
+          }
           const uint32_t ahead = item + (uint32_t)w.prefetch;
           if (w.prefetch > 0 && ahead < total) {
             const int s2 = (int)(ahead / (uint32_t)ntiles);
@@ -980,8 +1002,9 @@ __global__ void __launch_bounds__(C::NT, (wave_blocks<C, TP, TF, TC>()))
                     tile, buf);
     __syncthreads();  // every thread's stores are issued and the buffer is free
     if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(w.sync + 1 + tile_row(a, tile), 1u);
+      // publish the tile (release: the CTA's stores, ordered before by the barrier)
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(w.sync + 1 + tile_row(a, tile))
+                   : "memory");
     }
   }
 }

@@ -54,7 +54,7 @@ def _run(fields, step0, nsteps, static):
     import torch
     from pyfds_gb300 import _capi
     lib = _capi.load()
-    plans = [f._engine().prepare(step0, nsteps) for f in fields]
+    plans = [f._engine().prepare(step0, nsteps, batched=True) for f in fields]
     probs, states, tables = _structs(fields, plans)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     if static:
@@ -101,7 +101,7 @@ def test_static_scratch_rejects_a_capturing_stream(gpu):
     from pyfds_gb300 import _capi
     lib = _capi.load()
     _, fields = _fields()
-    plans = [f._engine().prepare(0, 1) for f in fields]
+    plans = [f._engine().prepare(0, 1, batched=True) for f in fields]
     probs, states, tables = _structs(fields, plans)
     side = torch.cuda.Stream()
     scratch = torch.zeros(16, device="cuda")
@@ -122,7 +122,7 @@ def test_static_scratch_rejects_oversized_batches(gpu):
     from pyfds_gb300 import _capi
     lib = _capi.load()
     specs, fields = _fields()
-    plans = [f._engine().prepare(0, 1) for f in fields]
+    plans = [f._engine().prepare(0, 1, batched=True) for f in fields]
     probs, states, tables = _structs(fields, plans)
     # a batch far larger than the built-in scratch (repeat one field many times)
     n = 4000
