@@ -136,6 +136,9 @@ typedef struct FdsStagProblem {
                      boundary values / outputs are shifted by the caller. 0 otherwise */
   const int64_t* flow_period; /* FDS_FLAG_FLOW: [ny] device array of shift periods in
                                  steps, int(dx / flow / dt) per row; NULL otherwise */
+  const int64_t* flow_period_host; /* FDS_FLAG_FLOW, optional: the same periods in host
+                                      memory; steps on which no row is due then skip
+                                      the shift launch and step as a field at rest */
 } FdsStagProblem;
 
 /*

@@ -74,7 +74,8 @@ class FdsStagProblem(C.Structure):
     _fields_ = [("family", C.c_int32), ("precision", C.c_int32), ("flags", C.c_uint32),
                 ("nx", C.c_int32), ("ny", C.c_int32), ("tile_x", C.c_int32),
                 ("tile_y", C.c_int32), ("stages", C.c_int32), ("coefs", FdsCoefs),
-                ("offset", C.c_double), ("flow_period", C.c_void_p)]
+                ("offset", C.c_double), ("flow_period", C.c_void_p),
+                ("flow_period_host", C.c_void_p)]
 
 
 class FdsStagState(C.Structure):

@@ -509,6 +509,7 @@ class StagEngine:
             setattr(prob.coefs, name, t.data_ptr() if t is not None else None)
         if prob.flags & _capi.FLAG_FLOW:
             prob.flow_period = self._flow_periods(torch, dev).data_ptr()
+            prob.flow_period_host = self._flow_cache[0].ctypes.data  # kept by the cache
         if self.status is None:
             self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         tstruct = self._tables_struct(tabs, outs, nsteps)

@@ -593,6 +593,61 @@ __device__ __forceinline__ bool tma_finish_tile(const StagCore<TP, TF, TC>& a, i
   return true;
 }
 
+// New potential of the cell in slot ps from the new fluxes around it (x: ps, ps + 1;
+// y: ps, ps + RX) and the potential update factors; x is the cell's column (the
+// radius of the exact axisymmetric scaling). The reference's operation order in
+// exact mode; fused multiply-adds otherwise.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TP potential_cell(const StagCore<TP, TF, TC>& a, const TP* sP,
+                                             const TF* sU, const TF* sV, const TC* sKx,
+                                             const TC* sKy, int ps, int x) {
+  const TF u = sU[ps];
+  const TF un1 = sU[ps + 1];
+  TF v = TF(0), vn1 = TF(0), kyi = TF(0), kyn = TF(0);
+  if constexpr (C::HAS_V) {
+    v = sV[ps];
+    vn1 = sV[ps + C::RX];
+    kyi = (TF)sKy[ps];
+    kyn = (TF)sKy[ps + C::RX];
+  }
+  const TF kxi = (TF)sKx[ps];
+  const TF kxn = (TF)sKx[ps + 1];
+  if constexpr (C::EXACT) {
+    TF w = u, wn = un1;
+    if constexpr (C::AXI) {
+      // a_p_vx.dot(vx * r): the flux is scaled by the radius of its column
+      const int xn = (x + 1 == a.nx) ? 0 : x + 1;
+      w = xmul(u, (TF)ldg_t(a.rx + x));
+      wn = xmul(un1, (TF)ldg_t(a.rx + xn));
+    }
+    // forward difference, offsets [0, s]: (0 + (-k)*w) + kn*wn
+    TF sx = xadd(-xmul(kxi, w), xmul(kxn, wn));
+    if constexpr (C::HAS_V) {
+      const TF sy = xadd(-xmul(kyi, v), xmul(kyn, vn1));
+      sx = xadd(sx, sy);
+    }
+    return (TP)xsub((TF)sP[ps], sx);
+  } else if constexpr (sizeof(TP) == sizeof(TF)) {
+    TF acc = (TF)sP[ps];
+    acc = fma(kxi, u, acc);
+    acc = fma(-kxn, un1, acc);
+    if constexpr (C::HAS_V) {
+      acc = fma(kyi, v, acc);
+      acc = fma(-kyn, vn1, acc);
+    }
+    return (TP)settle(acc);
+  } else {
+    // float increment accumulated into a float64 potential
+    TF inc = kxi * u;
+    inc = fma(-kxn, un1, inc);
+    if constexpr (C::HAS_V) {
+      inc = fma(kyi, v, inc);
+      inc = fma(-kyn, vn1, inc);
+    }
+    return sP[ps] + (TP)inc;
+  }
+}
+
 // Everything after the region has landed: flux update, flux bounds and probes,
 // potential update, next step's potential bounds and probes, stores.
 //
@@ -708,56 +763,11 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
     const int ps = pos[k];
     pn[k] = TP(0);
     if (own[k]) {
-      const TF u = sU[ps];
-      const TF un1 = sU[ps + 1];
-      TF v = TF(0), vn1 = TF(0), kyi = TF(0), kyn = TF(0);
-      if constexpr (C::HAS_V) {
-        v = sV[ps];
-        vn1 = sV[ps + RX];
-        kyi = (TF)sKy[ps];
-        kyn = (TF)sKy[ps + RX];
-      }
       if (si.store_flux) {
-        a.u_out[fo[k]] = u;
-        if constexpr (C::HAS_V) a.v_out[fo[k]] = v;
+        a.u_out[fo[k]] = sU[ps];
+        if constexpr (C::HAS_V) a.v_out[fo[k]] = sV[ps];
       }
-      const TF kxi = (TF)sKx[ps];
-      const TF kxn = (TF)sKx[ps + 1];
-      if constexpr (C::EXACT) {
-        TF w = u, wn = un1;
-        if constexpr (C::AXI) {
-          // a_p_vx.dot(vx * r): the flux is scaled by the radius of its column
-          const int x = xo[k];
-          const int xn = (x + 1 == a.nx) ? 0 : x + 1;
-          w = xmul(u, (TF)ldg_t(a.rx + x));
-          wn = xmul(un1, (TF)ldg_t(a.rx + xn));
-        }
-        // forward difference, offsets [0, s]: (0 + (-k)*w) + kn*wn
-        TF sx = xadd(-xmul(kxi, w), xmul(kxn, wn));
-        if constexpr (C::HAS_V) {
-          const TF sy = xadd(-xmul(kyi, v), xmul(kyn, vn1));
-          sx = xadd(sx, sy);
-        }
-        pn[k] = (TP)xsub((TF)sP[ps], sx);
-      } else if constexpr (sizeof(TP) == sizeof(TF)) {
-        TF acc = (TF)sP[ps];
-        acc = fma(kxi, u, acc);
-        acc = fma(-kxn, un1, acc);
-        if constexpr (C::HAS_V) {
-          acc = fma(kyi, v, acc);
-          acc = fma(-kyn, vn1, acc);
-        }
-        pn[k] = (TP)settle(acc);
-      } else {
-        // float increment accumulated into a float64 potential
-        TF inc = kxi * u;
-        inc = fma(-kxn, un1, inc);
-        if constexpr (C::HAS_V) {
-          inc = fma(kyi, v, inc);
-          inc = fma(-kyn, vn1, inc);
-        }
-        pn[k] = sP[ps] + (TP)inc;
-      }
+      pn[k] = potential_cell<C>(a, sP, sU, sV, sKx, sKy, ps, xo[k]);
     }
   }
   // the next step's potential bounds and probes go through shared memory; a tile

@@ -11,6 +11,7 @@
 #include "fds_internal.h"
 #include "batch_kernel.cuh"
 #include "march_kernel.cuh"
+#include "resident_1d.cuh"
 #include "stag_kernel.cuh"
 
 namespace fds {
@@ -367,6 +368,65 @@ WaveRun<TP, TF, TC> pick_wave(int family, int tx, int ty) {
   return nullptr;
 }
 
+// Every step of a call of a 1-D field in one CTA (stag_1d_resident_kernel): the
+// first step's potential bounds and probes in the prologue, then one launch.
+template <class C, typename TP, typename TF, typename TC>
+int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
+                     int64_t step0, int32_t nsteps, cudaStream_t stream) {
+  const int n = (int)a.n;
+  const size_t smem = resident_smem<TP, TF, TC>(n);
+  LaunchShape ls;
+  const int32_t rc =
+      kernel_shape<stag_1d_resident_kernel<C, TP, TF, TC>>(smem, kResidentThreads, false, &ls);
+  if (rc != FDS_OK) return rc;
+  const FdsCompTables& t0 = tabs->comp[0];
+  if (t0.bound_tile_start || t0.probe_tile_start) {
+    stag_prologue_kernel<TP><<<1, 1024, 0, stream>>>((TP*)st->cur[0], t0, tabs->pool, step0,
+                                                      a.ntiles, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
+  }
+  a.p_in = (const TP*)st->cur[0];
+  a.u_in = (const TF*)st->cur[1];
+  a.step = step0;
+  // the state ends where nsteps ping-pong swaps leave it
+  const bool odd = (nsteps & 1) != 0;
+  TP* p_fin = (TP*)(odd ? st->nxt[0] : st->cur[0]);
+  TF* u_fin = (TF*)(odd ? st->nxt[1] : st->cur[1]);
+  stag_1d_resident_kernel<C, TP, TF, TC><<<1, kResidentThreads, smem, stream>>>(a, nsteps, p_fin,
+                                                                              u_fin);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "1-D launch: %s", cudaGetErrorString(e));
+  if (odd)
+    for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+  return FDS_OK;
+}
+
+template <typename TP, typename TF, typename TC>
+using ResidentRun = int32_t (*)(StagArgs<TP, TF, TC>&, FdsStagState*, const FdsStagTables*,
+                                int64_t, int32_t, cudaStream_t);
+
+template <typename TP, typename TF, typename TC, bool ALLOW_EXACT, bool ALLOW_ACOUSTIC>
+ResidentRun<TP, TF, TC> pick_resident(int family, bool absorb, bool exact) {
+  if (exact && !ALLOW_EXACT) return nullptr;
+  const bool acoustic = family == FDS_FAMILY_ACOUSTIC;
+#define FDS_PICK_RES(MEM, ABS, EX)                                                          \
+  if (acoustic == MEM && absorb == ABS && exact == EX)                                      \
+    return &run_resident<StagCfg<kTile1dX, 1, kThreads, false, MEM, ABS, false, EX>, TP, TF, TC>;
+  if constexpr (ALLOW_ACOUSTIC) {
+    FDS_PICK_RES(true, false, false)
+    FDS_PICK_RES(true, true, false)
+    if constexpr (ALLOW_EXACT) {
+      FDS_PICK_RES(true, false, true)
+      FDS_PICK_RES(true, true, true)
+    }
+  }
+  FDS_PICK_RES(false, false, false)
+  if constexpr (ALLOW_EXACT) FDS_PICK_RES(false, false, true)
+#undef FDS_PICK_RES
+  return nullptr;
+}
+
 template <typename TP, typename TF, typename TC, bool ALLOW_EXACT, bool ALLOW_ACOUSTIC>
 int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsStagTables* tabs,
                        int64_t step0, int32_t nsteps, int32_t store_flux, cudaStream_t stream) {
@@ -435,6 +495,14 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   tma.state[4] = st->cur[2];
   tma.state[5] = st->nxt[2];
 
+  // a 1-D field that fits one CTA's shared memory: every step in one launch (stages 0
+  // or 4; stages 1 keeps one launch per step)
+  if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4) && a.n <= kResidentMaxCells &&
+      resident_smem<TP, TF, TC>((int)a.n) <= 227 * 1024) {
+    ResidentRun<TP, TF, TC> rr =
+        pick_resident<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, absorb, exact);
+    if (rr) return rr(a, st, tabs, step0, nsteps, stream);
+  }
   if (prob->stages == 4 && has_v && !absorb && !exact && !flow) {
     WaveRun<TP, TF, TC> wr =
         pick_wave<TP, TF, TC, ALLOW_ACOUSTIC>(prob->family, prob->tile_x, prob->tile_y);
@@ -452,6 +520,22 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
   }
+  // a moving medium with a host copy of its shift periods: steps on which no row is
+  // due need neither the shift launch nor the prologue after it (the periods that
+  // occur, deduplicated; numpy's step % f == 0, f == 0 always due)
+  std::vector<int64_t> periods;
+  if (flow && prob->flow_period_host) {
+    periods.assign(prob->flow_period_host, prob->flow_period_host + prob->ny);
+    std::sort(periods.begin(), periods.end());
+    periods.erase(std::unique(periods.begin(), periods.end()), periods.end());
+  }
+  auto shift_due = [&](int64_t step) {
+    if (!flow) return false;
+    if (!prob->flow_period_host) return true;
+    for (const int64_t f : periods)
+      if (f == 0 || step % f == 0) return true;
+    return false;
+  };
   for (int32_t s = 0; s < nsteps;) {
     // the two-step kernel advances two steps per launch (one for an odd last step)
     const int take = (two_step && s + 1 < nsteps) ? 2 : 1;
@@ -465,14 +549,15 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
     a.step = step0 + s;
     // a moving medium shifts rows between the pressure update and the next step's
     // pressure bounds / probes, which then run in the prologue kernel instead
-    a.apply_next = (s + take < nsteps && !flow) ? 1 : 0;
+    const bool due = shift_due(step0 + s);
+    a.apply_next = (s + take < nsteps && !due) ? 1 : 0;
     a.store_flux = (store_flux || s + take == nsteps) ? 1 : 0;
     const int32_t rc = fn(a, stream, &tma);
     if (rc != FDS_OK) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "step launch: %s", cudaGetErrorString(e));
     for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
-    if (flow) {
+    if (due) {
       const int32_t rf = launch_flow_shift(prob, st->cur, step0 + s, stream);
       if (rf != FDS_OK) return rf;
       if (s + 1 < nsteps && (t0.bound_tile_start || t0.probe_tile_start)) {

@@ -42,7 +42,7 @@ def test_abi_version(lib):
 
 def test_struct_layouts_match_header():
     assert C.sizeof(_capi.FdsCoefs) == 11 * 8
-    assert C.sizeof(_capi.FdsStagProblem) == 8 * 4 + 11 * 8 + 8 + 8
+    assert C.sizeof(_capi.FdsStagProblem) == 8 * 4 + 11 * 8 + 8 + 8 + 8
     assert C.sizeof(_capi.FdsStagState) == 6 * 8
     assert C.sizeof(_capi.FdsCompTables) == 6 * 8 + 8
     assert C.sizeof(_capi.FdsStagTables) == 3 * 56 + 40
