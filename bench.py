@@ -954,9 +954,13 @@ def run_ours(args):
     if kernel_status:
         raise RuntimeError("a kernel reported status 0x%x during the timed runs" % kernel_status)
     st_used = eng.stages()
+    from pyfds_gb300 import _capi as _c
+    # a 1-D field of at most 4096 cells runs every step of a call in one launch
+    resident_1d = (args.workload != "nonlinear1d" and cells <= 4096 and st_used in (0, 4)
+                   and not field._stag_flags() & _c.FLAG_HAS_V)
     # steps per launch: two with two steps per tile, every step of the call for the
     # wavefront kernel (stages 4, one launch per simulate call), else one
-    spl = 2 if st_used == 3 else (nt if st_used == 4 else 1)
+    spl = 2 if st_used == 3 else (nt if st_used == 4 or resident_1d else 1)
     launch_ms = step_kernel_ms * spl
     ref_outs = [o.cpu().numpy() if o is not None else None for o in plan["outs"]]
     dword = None
@@ -1036,6 +1040,8 @@ def run_ours(args):
                                     "nonlinear1d": "nl1d_kernel (every step in one launch; the "
                                                    "field stays in L1/L2)"}.get(
                                         args.workload,
+                                        "stag_1d_resident_kernel (every step of the call "
+                                        "in one CTA)" if resident_1d else
                                         {3: "stag_tb2_kernel", 4: "stag_wave_kernel (every "
                                          "step of the call in one launch)"}.get(
                                             st_used, "stag_step_kernel")),
@@ -1047,7 +1053,7 @@ def run_ours(args):
             "gpu_launches": int(args.steps * (nt + 1 + 2 * _flow_due_steps(field, nt)
                                               if args.workload == "flow" else
                                               1 if args.workload == "nonlinear1d" else
-                                              2 if st_used == 4 else
+                                              2 if st_used == 4 or resident_1d else
                                               (nt + spl - 1) // spl + 1))}
     if dword is not None:
         line["double_word"] = dword

@@ -374,7 +374,14 @@ template <class C, typename TP, typename TF, typename TC>
 int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
                      int64_t step0, int32_t nsteps, cudaStream_t stream) {
   const int n = (int)a.n;
-  const size_t smem = resident_smem<TP, TF, TC>(n);
+  // state and coefficients, the table area, and the signal pool when it fits
+  size_t smem = resident_smem<TP, TF, TC>(n) + kResidentTableBytes;
+  int64_t pool_cached = 0;
+  if (tabs->pool && tabs->pool_len > 0 &&
+      smem + (size_t)tabs->pool_len * sizeof(double) <= kResidentMaxSmem) {
+    pool_cached = tabs->pool_len;
+    smem += (size_t)pool_cached * sizeof(double);
+  }
   LaunchShape ls;
   const int32_t rc =
       kernel_shape<stag_1d_resident_kernel<C, TP, TF, TC>>(smem, kResidentThreads, false, &ls);
@@ -393,8 +400,8 @@ int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTab
   const bool odd = (nsteps & 1) != 0;
   TP* p_fin = (TP*)(odd ? st->nxt[0] : st->cur[0]);
   TF* u_fin = (TF*)(odd ? st->nxt[1] : st->cur[1]);
-  stag_1d_resident_kernel<C, TP, TF, TC><<<1, kResidentThreads, smem, stream>>>(a, nsteps, p_fin,
-                                                                              u_fin);
+  stag_1d_resident_kernel<C, TP, TF, TC><<<1, kResidentThreads, smem, stream>>>(
+      a, nsteps, p_fin, u_fin, pool_cached);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "1-D launch: %s", cudaGetErrorString(e));
   if (odd)
@@ -498,7 +505,7 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   // a 1-D field that fits one CTA's shared memory: every step in one launch (stages 0
   // or 4; stages 1 keeps one launch per step)
   if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4) && a.n <= kResidentMaxCells &&
-      resident_smem<TP, TF, TC>((int)a.n) <= 227 * 1024) {
+      resident_smem<TP, TF, TC>((int)a.n) + kResidentTableBytes <= kResidentMaxSmem) {
     ResidentRun<TP, TF, TC> rr =
         pick_resident<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, absorb, exact);
     if (rr) return rr(a, st, tabs, step0, nsteps, stream);
