@@ -593,25 +593,15 @@ __device__ __forceinline__ bool tma_finish_tile(const StagCore<TP, TF, TC>& a, i
   return true;
 }
 
-// New potential of the cell in slot ps from the new fluxes around it (x: ps, ps + 1;
-// y: ps, ps + RX) and the potential update factors; x is the cell's column (the
-// radius of the exact axisymmetric scaling). The reference's operation order in
-// exact mode; fused multiply-adds otherwise.
+// New potential of a cell from its old potential p, the new fluxes around it (x: u
+// at the cell, un1 at its right neighbour; y: v at the cell, vn1 at the cell below)
+// and the potential update factors; x is the cell's column (the radius of the exact
+// axisymmetric scaling). The reference's operation order in exact mode; fused
+// multiply-adds otherwise.
 template <class C, typename TP, typename TF, typename TC>
-__device__ __forceinline__ TP potential_cell(const StagCore<TP, TF, TC>& a, const TP* sP,
-                                             const TF* sU, const TF* sV, const TC* sKx,
-                                             const TC* sKy, int ps, int x) {
-  const TF u = sU[ps];
-  const TF un1 = sU[ps + 1];
-  TF v = TF(0), vn1 = TF(0), kyi = TF(0), kyn = TF(0);
-  if constexpr (C::HAS_V) {
-    v = sV[ps];
-    vn1 = sV[ps + C::RX];
-    kyi = (TF)sKy[ps];
-    kyn = (TF)sKy[ps + C::RX];
-  }
-  const TF kxi = (TF)sKx[ps];
-  const TF kxn = (TF)sKx[ps + 1];
+__device__ __forceinline__ TP potential_regs(const StagCore<TP, TF, TC>& a, TP p, TF u, TF un1,
+                                             TF v, TF vn1, TF kxi, TF kxn, TF kyi, TF kyn,
+                                             int x) {
   if constexpr (C::EXACT) {
     TF w = u, wn = un1;
     if constexpr (C::AXI) {
@@ -626,9 +616,9 @@ __device__ __forceinline__ TP potential_cell(const StagCore<TP, TF, TC>& a, cons
       const TF sy = xadd(-xmul(kyi, v), xmul(kyn, vn1));
       sx = xadd(sx, sy);
     }
-    return (TP)xsub((TF)sP[ps], sx);
+    return (TP)xsub((TF)p, sx);
   } else if constexpr (sizeof(TP) == sizeof(TF)) {
-    TF acc = (TF)sP[ps];
+    TF acc = (TF)p;
     acc = fma(kxi, u, acc);
     acc = fma(-kxn, un1, acc);
     if constexpr (C::HAS_V) {
@@ -644,8 +634,24 @@ __device__ __forceinline__ TP potential_cell(const StagCore<TP, TF, TC>& a, cons
       inc = fma(kyi, v, inc);
       inc = fma(-kyn, vn1, inc);
     }
-    return sP[ps] + (TP)inc;
+    return p + (TP)inc;
   }
+}
+
+// potential_regs with every operand read from the staged slots around slot ps.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TP potential_cell(const StagCore<TP, TF, TC>& a, const TP* sP,
+                                             const TF* sU, const TF* sV, const TC* sKx,
+                                             const TC* sKy, int ps, int x) {
+  TF v = TF(0), vn1 = TF(0), kyi = TF(0), kyn = TF(0);
+  if constexpr (C::HAS_V) {
+    v = sV[ps];
+    vn1 = sV[ps + C::RX];
+    kyi = (TF)sKy[ps];
+    kyn = (TF)sKy[ps + C::RX];
+  }
+  return potential_regs<C>(a, sP[ps], sU[ps], sU[ps + 1], v, vn1, (TF)sKx[ps], (TF)sKx[ps + 1],
+                           kyi, kyn, x);
 }
 
 // Everything after the region has landed: flux update, flux bounds and probes,
@@ -663,6 +669,14 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   constexpr int OIT = TX * TY / NT;
   static_assert((TX & (TX - 1)) == 0, "tile width must be a power of two");
   static_assert((TX * TY) % NT == 0, "the tile's cells must divide evenly among threads");
+  // float64 (bound by the FP64 pipe) keeps the cells' potential and new fluxes in
+  // registers for the potential update instead of reloading them from shared memory,
+  // and on 2-D tiles gives each thread OIT consecutive rows of one column, so that
+  // the flux below a cell is mostly the thread's own register. The other precisions
+  // (bound by instruction issue) keep cells NT apart and reload: the registers would
+  // spill (double-word two-step kernel: 8 -> 56 bytes)
+  constexpr bool REGS = std::is_same<TF, double>::value && std::is_same<TP, double>::value;
+  constexpr bool ROWS = REGS && C::HAS_V && NT % TX == 0;
   static_assert(!C::HAS_V || TX + TY <= NT, "halo threads: TX + TY must not exceed NT");
   TP* sP = b.P;
   TF* sU = b.U;
@@ -681,11 +695,12 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   int64_t fo[OIT];
   int xo[OIT];
   bool own[OIT], inu[OIT], inv[OIT];
+  // ROWS: thread t owns column t % TX, rows (t / TX) * OIT .. + OIT - 1; else cells
+  // t, t + NT, ...
 #pragma unroll
   for (int k = 0; k < OIT; ++k) {
-    const int c = tid + NT * k;
-    const int lx = c % TX;
-    const int ly = c / TX;
+    const int lx = ROWS ? tid % TX : (tid + NT * k) % TX;
+    const int ly = ROWS ? (tid / TX) * OIT + k : (tid + NT * k) / TX;
     const int x = x0 + lx;
     const int y = y0 + ly;
     pos[k] = (ly + OY) * RX + lx + C::OX;
@@ -705,6 +720,11 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
   const int64_t hv_f = (int64_t)y1 * a.nx + x0 + hv_lx;
 
   // ---- new fluxes over U-ext and V-ext ----
+  TP po[OIT];  // (REGS) the cells' potential after this step's bounds
+  if constexpr (REGS) {
+#pragma unroll
+    for (int k = 0; k < OIT; ++k) po[k] = sP[pos[k]];
+  }
   TF un[OIT], vn[OIT];
 #pragma unroll
   for (int k = 0; k < OIT; ++k) {
@@ -752,6 +772,14 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
     apply_bound_groups<NT>(a.tab[1], tile, sU, a.pool, si.step);
     if constexpr (C::HAS_V) apply_bound_groups<NT>(a.tab[2], tile, sV, a.pool, si.step);
     __syncthreads();
+    // the bounds may have changed the fluxes held in registers
+    if constexpr (REGS) {
+#pragma unroll
+      for (int k = 0; k < OIT; ++k) {
+        un[k] = sU[pos[k]];
+        if constexpr (C::HAS_V) vn[k] = sV[pos[k]];
+      }
+    }
   }
   write_probes<NT>(a.tab[1], tile, sU, si.step - si.step0);
   if constexpr (C::HAS_V) write_probes<NT>(a.tab[2], tile, sV, si.step - si.step0);
@@ -763,11 +791,27 @@ __device__ __forceinline__ void compute_tile(const StagCore<TP, TF, TC>& a, cons
     const int ps = pos[k];
     pn[k] = TP(0);
     if (own[k]) {
-      if (si.store_flux) {
-        a.u_out[fo[k]] = sU[ps];
-        if constexpr (C::HAS_V) a.v_out[fo[k]] = sV[ps];
+      if constexpr (REGS) {
+        if (si.store_flux) {
+          a.u_out[fo[k]] = un[k];
+          if constexpr (C::HAS_V) a.v_out[fo[k]] = vn[k];
+        }
+        // the flux below the cell: this thread's next row, or the slot past its rows
+        TF vb = TF(0), kyi = TF(0), kyn = TF(0);
+        if constexpr (C::HAS_V) {
+          vb = (ROWS && k + 1 < OIT) ? vn[(k + 1) % OIT] : sV[ps + RX];
+          kyi = (TF)sKy[ps];
+          kyn = (TF)sKy[ps + RX];
+        }
+        pn[k] = potential_regs<C>(a, po[k], un[k], sU[ps + 1], vn[k], vb, (TF)sKx[ps],
+                                  (TF)sKx[ps + 1], kyi, kyn, xo[k]);
+      } else {
+        if (si.store_flux) {
+          a.u_out[fo[k]] = sU[ps];
+          if constexpr (C::HAS_V) a.v_out[fo[k]] = sV[ps];
+        }
+        pn[k] = potential_cell<C>(a, sP, sU, sV, sKx, sKy, ps, xo[k]);
       }
-      pn[k] = potential_cell<C>(a, sP, sU, sV, sKx, sKy, ps, xo[k]);
     }
   }
   // the next step's potential bounds and probes go through shared memory; a tile
