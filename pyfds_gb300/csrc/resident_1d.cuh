@@ -169,15 +169,19 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
   for (int32_t s = 0; s < nsteps; ++s) {
     const int64_t step = a.step + s;
     // ---- new flux of every cell ----
+    // (slots k past the field are skipped as a whole: the same branch for every
+    // thread, so no predicated-off FP64 instructions occupy the pipe)
     TF un[CPT];
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
+      if (k * kResidentThreads >= n) break;
       const int i = tid + k * kResidentThreads;
       un[k] = i < n ? flux_new<C, true>(a, sP, sU, sB, i + 1, (int64_t)i, i) : TF(0);
     }
     if constexpr (C::MEMORY && C::ABSORB) __syncthreads();  // neighbours read the old flux
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
+      if (k * kResidentThreads >= n) break;
       const int i = tid + k * kResidentThreads;
       if (i < n) sU[i + 1] = un[k];
     }
@@ -191,11 +195,13 @@ __global__ void __launch_bounds__(kResidentThreads, 1)
     TP pn[CPT];
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
+      if (k * kResidentThreads >= n) break;
       const int i = tid + k * kResidentThreads;
       pn[k] = i < n ? potential_cell<C>(a, sP, sU, sU, sK, sK, i + 1, i) : TP(0);
     }
 #pragma unroll
     for (int k = 0; k < CPT; ++k) {
+      if (k * kResidentThreads >= n) break;
       const int i = tid + k * kResidentThreads;
       if (i < n) sP[i + 1] = pn[k];
     }
