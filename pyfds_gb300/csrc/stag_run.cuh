@@ -11,6 +11,7 @@
 #include "fds_internal.h"
 #include "batch_kernel.cuh"
 #include "march_kernel.cuh"
+#include "cluster_1d.cuh"
 #include "resident_1d.cuh"
 #include "stag_kernel.cuh"
 
@@ -372,7 +373,7 @@ WaveRun<TP, TF, TC> pick_wave(int family, int tx, int ty) {
 // first step's potential bounds and probes in the prologue, then one launch.
 template <class C, typename TP, typename TF, typename TC>
 int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
-                     int64_t step0, int32_t nsteps, cudaStream_t stream) {
+                     int64_t step0, int32_t nsteps, cudaStream_t stream, int) {
   const int n = (int)a.n;
   // state and coefficients, the table area, and the signal pool when it fits
   size_t smem = resident_smem<TP, TF, TC>(n) + kResidentTableBytes;
@@ -409,17 +410,89 @@ int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTab
   return FDS_OK;
 }
 
+// Every step of a call of a 1-D field spread over one thread-block cluster of `ncta`
+// CTAs (stag_1d_cluster_kernel): the prologue, then one cluster launch.
+template <class C, typename TP, typename TF, typename TC>
+int32_t run_cluster(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
+                    int64_t step0, int32_t nsteps, cudaStream_t stream, int ncta) {
+  const int n = (int)a.n;
+  const int m = (n + ncta - 1) / ncta;
+  ncta = (n + m - 1) / m;  // every CTA owns at least one cell
+  size_t smem = resident_smem<TP, TF, TC>(m) + kResidentTableBytes;
+  int64_t pool_cached = 0;
+  if (tabs->pool && tabs->pool_len > 0 &&
+      smem + (size_t)tabs->pool_len * sizeof(double) <= kResidentMaxSmem) {
+    pool_cached = tabs->pool_len;
+    smem += (size_t)pool_cached * sizeof(double);
+  }
+  LaunchShape ls;
+  const int32_t rc =
+      kernel_shape<stag_1d_cluster_kernel<C, TP, TF, TC>>(smem, kClusterThreads, false, &ls);
+  if (rc != FDS_OK) return rc;
+  const FdsCompTables& t0 = tabs->comp[0];
+  if (t0.bound_tile_start || t0.probe_tile_start) {
+    stag_prologue_kernel<TP><<<1, 1024, 0, stream>>>((TP*)st->cur[0], t0, tabs->pool, step0,
+                                                      a.ntiles, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "prologue launch: %s", cudaGetErrorString(e));
+  }
+  a.p_in = (const TP*)st->cur[0];
+  a.u_in = (const TF*)st->cur[1];
+  a.step = step0;
+  const bool odd = (nsteps & 1) != 0;
+  TP* p_fin = (TP*)(odd ? st->nxt[0] : st->cur[0]);
+  TF* u_fin = (TF*)(odd ? st->nxt[1] : st->cur[1]);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ncta, 1, 1);
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, stag_1d_cluster_kernel<C, TP, TF, TC>, a,
+                                           nsteps, p_fin, u_fin, pool_cached, (int32_t)m);
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "1-D cluster launch: %s", cudaGetErrorString(e));
+  if (odd)
+    for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+  return FDS_OK;
+}
+
+// Cells per CTA below which a 1-D field stays in one CTA (a cluster of CTAs of at
+// least this many cells each otherwise, up to the portable cluster size)
+constexpr int kClusterMinCellsPerCta = 128;
+
+// A 1-D field of n cells: in one cluster (ncta > 1), in one CTA (ncta == 1), or not
+// resident at all (0, one launch per step).
+template <typename TP, typename TF, typename TC>
+int resident_ctas(int64_t n) {
+  if (n >= 2 * kClusterMinCellsPerCta && n <= (int64_t)kClusterMaxCta * kClusterMaxCellsPerCta) {
+    const int ncta = (int)std::min<int64_t>(kClusterMaxCta,
+                                            (n + kClusterMinCellsPerCta - 1) / kClusterMinCellsPerCta);
+    const int m = (int)((n + ncta - 1) / ncta);
+    if (resident_smem<TP, TF, TC>(m) + kResidentTableBytes <= kResidentMaxSmem) return ncta;
+  }
+  if (n <= kResidentMaxCells && resident_smem<TP, TF, TC>((int)n) + kResidentTableBytes <= kResidentMaxSmem)
+    return 1;
+  return 0;
+}
+
 template <typename TP, typename TF, typename TC>
 using ResidentRun = int32_t (*)(StagArgs<TP, TF, TC>&, FdsStagState*, const FdsStagTables*,
-                                int64_t, int32_t, cudaStream_t);
+                                int64_t, int32_t, cudaStream_t, int);
 
 template <typename TP, typename TF, typename TC, bool ALLOW_EXACT, bool ALLOW_ACOUSTIC>
-ResidentRun<TP, TF, TC> pick_resident(int family, bool absorb, bool exact) {
+ResidentRun<TP, TF, TC> pick_resident(int family, bool absorb, bool exact, bool cluster) {
   if (exact && !ALLOW_EXACT) return nullptr;
   const bool acoustic = family == FDS_FAMILY_ACOUSTIC;
 #define FDS_PICK_RES(MEM, ABS, EX)                                                          \
   if (acoustic == MEM && absorb == ABS && exact == EX)                                      \
-    return &run_resident<StagCfg<kTile1dX, 1, kThreads, false, MEM, ABS, false, EX>, TP, TF, TC>;
+    return cluster ? &run_cluster<StagCfg<kTile1dX, 1, kThreads, false, MEM, ABS, false, EX>, TP, TF, TC> \
+                   : &run_resident<StagCfg<kTile1dX, 1, kThreads, false, MEM, ABS, false, EX>, TP, TF, TC>;
   if constexpr (ALLOW_ACOUSTIC) {
     FDS_PICK_RES(true, false, false)
     FDS_PICK_RES(true, true, false)
@@ -502,13 +575,16 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   tma.state[4] = st->cur[2];
   tma.state[5] = st->nxt[2];
 
-  // a 1-D field that fits one CTA's shared memory: every step in one launch (stages 0
-  // or 4; stages 1 keeps one launch per step)
-  if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4) && a.n <= kResidentMaxCells &&
-      resident_smem<TP, TF, TC>((int)a.n) + kResidentTableBytes <= kResidentMaxSmem) {
+  // a 1-D field that fits shared memory: every step in one launch, on a cluster of
+  // CTAs from 256 cells on, else on one CTA (stages 0 or 4; stages 1 keeps one launch
+  // per step)
+  if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4)) {
+    const int ncta = resident_ctas<TP, TF, TC>(a.n);
     ResidentRun<TP, TF, TC> rr =
-        pick_resident<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, absorb, exact);
-    if (rr) return rr(a, st, tabs, step0, nsteps, stream);
+        ncta > 0 ? pick_resident<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, absorb,
+                                                                           exact, ncta > 1)
+                 : nullptr;
+    if (rr) return rr(a, st, tabs, step0, nsteps, stream, ncta);
   }
   if (prob->stages == 4 && has_v && !absorb && !exact && !flow) {
     WaveRun<TP, TF, TC> wr =
