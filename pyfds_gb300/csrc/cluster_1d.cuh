@@ -18,8 +18,19 @@
 // hl[] / hr[] hold them, double-buffered by step parity so that a neighbour can
 // write this step's flux while this CTA still reads the last one.) Two cluster
 // barriers per step order these writes after the reads they replace and before the
-// reads that need them. Every cell is computed by flux_new and potential_regs, the
-// tile kernel's arithmetic, so results are the tile kernel's bit for bit.
+// reads that need them.
+//
+// Without absorption one cluster barrier per step suffices: each CTA also computes
+// the flux of the cell right of its block (slot m_r + 1), from that cell's potential
+// (a halo value) and its own previous flux (which this CTA computed the step before),
+// with the same arithmetic and bounds as the owner does, so the potential update of
+// its last cell needs nothing from the neighbour. Only potentials cross CTAs: after
+// its potential update and bounds, a CTA writes its first and last potential into
+// the neighbours' halo slots pl[parity] / pr[parity], double-buffered so that a
+// neighbour still reading the last step's values is not overwritten.
+//
+// Every cell is computed by flux_new and potential_regs, the tile kernel's
+// arithmetic, so results are the tile kernel's bit for bit.
 #pragma once
 
 #include "resident_1d.cuh"
@@ -101,6 +112,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   constexpr int NT = kClusterThreads;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ TF hl[2], hr[2];  // old / new flux of the neighbour cells, by step parity
+  __shared__ TP pl[2], pr[2];  // potential of the neighbour cells, by step parity
+  constexpr bool ONE = !(C::MEMORY && C::ABSORB);  // one cluster barrier per step
   const int n = (int)a.n;
   const int ntiles = a.ntiles;
   const int rank = (int)blockIdx.x;  // the grid is one cluster
@@ -132,11 +145,16 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     pool = sp;
   }
   if (tid == 0) {
-    // the neighbours' fluxes before the first step (parity of step -1)
+    // the neighbours' fluxes and potentials before the first step (parity of step -1)
     hl[1] = sU[0];
     hr[1] = sU[mr + 1];
     hl[0] = hr[0] = TF(0);
+    pl[1] = sP[0];
+    pr[1] = sP[mr + 1];
+    pl[0] = pr[0] = TP(0);
   }
+  // ONE: this CTA also computes the flux of cell c1 (slot mr + 1) when it exists
+  const int nf = (ONE && c1 < n) ? mr + 1 : mr;
   const bool fb = rt[1].ngroups > 0;
   const bool fp = rt[1].nprobes > 0;
   const bool pb = rt[0].ngroups > 0;
@@ -146,6 +164,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
   for (int32_t s = 0; s < nsteps; ++s) {
     const int64_t step = a.step + s;
     const int cur = s & 1, old = cur ^ 1;
+    if constexpr (ONE) {
+      // the neighbours' potentials of the last step into the halo slots; each is read
+      // only by the thread that writes it here (cells c0 and c1 below)
+      if (tid == 0) sP[0] = pl[old];
+      if (nf > mr && tid == mr % NT) sP[mr + 1] = pr[old];
+    }
     if constexpr (C::MEMORY && C::ABSORB) {
       // the neighbours' fluxes of the last step, where the absorption term reads them
       if (tid == 0) {
@@ -155,33 +179,38 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       __syncthreads();
     }
     // ---- new flux of every owned cell ----
-    TF un[CPT];
+    // (CPT + 1 slots per thread: with ONE a CTA of the maximal block computes one flux
+    // past its cells)
+    TF un[CPT + 1];
 #pragma unroll
-    for (int k = 0; k < CPT; ++k) {
-      if (k * NT >= mr) break;
-      const int j = tid + k * NT;  // owned index; slot j + 1
-      un[k] = j < mr ? flux_new<C, true>(a, sP, sU, sB, j + 1, (int64_t)(c0 + j), c0 + j)
+    for (int k = 0; k < CPT + 1; ++k) {
+      if (k * NT >= nf) break;
+      const int j = tid + k * NT;  // owned index (mr: the cell right of the block); slot j + 1
+      un[k] = j < nf ? flux_new<C, true>(a, sP, sU, sB, j + 1, (int64_t)(c0 + j), c0 + j)
                      : TF(0);
     }
     if constexpr (C::MEMORY && C::ABSORB) __syncthreads();  // neighbours read the old flux
 #pragma unroll
-    for (int k = 0; k < CPT; ++k) {
-      if (k * NT >= mr) break;
+    for (int k = 0; k < CPT + 1; ++k) {
+      if (k * NT >= nf) break;
       const int j = tid + k * NT;
-      if (j < mr) sU[j + 1] = un[k];
+      if (j < nf) sU[j + 1] = un[k];
     }
     __syncthreads();
     if (fb) {
-      apply_bound_range(rt[1], sU, pool, step, c0, c1);
+      // ONE: the bounds of cell c1 too, where this CTA computed its flux
+      apply_bound_range(rt[1], sU, pool, step, c0, c0 + nf);
       __syncthreads();
     }
     if (fp) write_probe_range(rt[1], a.tab[1], sU, s, c0, c1);
-    // this step's flux of the first and last owned cells to the neighbours
-    if (tid == 0) {
-      if (rank > 0) st_cluster(&hr[cur], (uint32_t)(rank - 1), sU[1]);
-      if (rank + 1 < ncta) st_cluster(&hl[cur], (uint32_t)(rank + 1), sU[mr]);
+    if constexpr (!ONE) {
+      // this step's flux of the first and last owned cells to the neighbours
+      if (tid == 0) {
+        if (rank > 0) st_cluster(&hr[cur], (uint32_t)(rank - 1), sU[1]);
+        if (rank + 1 < ncta) st_cluster(&hl[cur], (uint32_t)(rank + 1), sU[mr]);
+      }
+      cluster_sync();
     }
-    cluster_sync();
     // ---- new potential of every owned cell (the last one reads the right
     // neighbour's new flux from hr[cur]; outside the field it stays 0) ----
     TP pn[CPT];
@@ -191,7 +220,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       const int j = tid + k * NT;
       if (j < mr) {
         const int ps = j + 1;
-        const TF un1 = (j + 1 == mr) ? hr[cur] : sU[ps + 1];
+        const TF un1 = (!ONE && j + 1 == mr) ? hr[cur] : sU[ps + 1];
         pn[k] = potential_regs<C>(a, sP[ps], sU[ps], un1, TF(0), TF(0), (TF)sK[ps],
                                   (TF)sK[ps + 1], TF(0), TF(0), c0 + j);
       } else {
@@ -212,8 +241,16 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       }
       if (pp) write_probe_range(rt[0], a.tab[0], sP, s + 1, c0, c1);
     }
-    // the last owned cell's potential to the right neighbour's left halo
-    if (tid == 0 && rank + 1 < ncta) st_cluster(&sP[0], (uint32_t)(rank + 1), sP[mr]);
+    if constexpr (ONE) {
+      // the first and last owned potentials to the neighbours' halo slots
+      if (tid == 0) {
+        if (rank > 0) st_cluster(&pr[cur], (uint32_t)(rank - 1), sP[1]);
+        if (rank + 1 < ncta) st_cluster(&pl[cur], (uint32_t)(rank + 1), sP[mr]);
+      }
+    } else {
+      // the last owned cell's potential to the right neighbour's left halo
+      if (tid == 0 && rank + 1 < ncta) st_cluster(&sP[0], (uint32_t)(rank + 1), sP[mr]);
+    }
     cluster_sync();
   }
   bool bad = false;
