@@ -576,9 +576,9 @@ int32_t run_stag_typed(const FdsStagProblem* prob, FdsStagState* st, const FdsSt
   tma.state[5] = st->nxt[2];
 
   // a 1-D field that fits shared memory: every step in one launch, on a cluster of
-  // CTAs from 256 cells on, else on one CTA (stages 0 or 4; stages 1 keeps one launch
-  // per step)
-  if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4)) {
+  // CTAs from 256 cells on, else on one CTA (stages 0 or 4, calls of two steps or more;
+  // stages 1 keeps one launch per step, and a single step is a tile-kernel launch)
+  if (!has_v && !flow && (prob->stages == 0 || prob->stages == 4) && nsteps > 1) {
     const int ncta = resident_ctas<TP, TF, TC>(a.n);
     ResidentRun<TP, TF, TC> rr =
         ncta > 0 ? pick_resident<TP, TF, TC, ALLOW_EXACT, ALLOW_ACOUSTIC>(prob->family, absorb,

@@ -66,12 +66,17 @@ extern "C" int32_t fds_thermoacoustic_run(
   if (!ac->coefs.bx) return set_error(FDS_E_ARG, "acoustic coefficients missing");
   const int n = ac->nx;
   cudaStream_t s = (cudaStream_t)stream;
+  // one step per field and call, between the coupling launches: the tile kernel
+  // (stages 1), not the kernels that keep a 1-D field in shared memory for a whole call
+  FdsStagProblem ac1 = *ac, th1 = *th;
+  ac1.stages = 1;
+  th1.stages = 1;
   for (int32_t k = 0; k < nsteps; ++k) {
     const int64_t step = step0 + k;
     FdsStagTables ta = step_tables(*act, k), tt = step_tables(*tht, k);
-    int32_t rc = fds_stag_run(ac, acs, &ta, step, 1, 1, stream);
+    int32_t rc = fds_stag_run(&ac1, acs, &ta, step, 1, 1, stream);
     if (rc != FDS_OK) return rc;
-    rc = fds_stag_run(th, ths, &tt, step, 1, 0, stream);
+    rc = fds_stag_run(&th1, ths, &tt, step, 1, 0, stream);
     if (rc != FDS_OK) return rc;
     const bool due = step % stepping == 0;
     int mode;
