@@ -288,59 +288,127 @@ __device__ __forceinline__ TF absorb_fma(const StagCore<TP, TF, TC>& a, const TF
   return acc;
 }
 
-// New flux at flat index i from the potential slots (pos, pos - back) and the
-// old flux; sB holds this direction's factors (slots of out-of-range cells hold 0).
-template <class C, bool IS_X, typename TP, typename TF, typename TC>
-__device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* sP, const TF* sF,
-                                       const TC* sB, int pos, int64_t i, int x) {
-  const int back = IS_X ? 1 : C::RX;
-  const TF b = (TF)sB[pos];
-  const TF bm = (TF)sB[pos - back];
-  const TF p = (TF)sP[pos];
-  const TF pm = (TF)sP[pos - back];
+// The new flux of a cell of a 1-D field from register operands: the potentials p_ of
+// the cell and pm_ of the cell before it, their factors b_ and bm_, the old flux u
+// and, with absorption, the old fluxes ul / ur of the neighbour cells and the
+// absorption diagonals am / a0 / ap at them (absorb_term's order). flux_new's
+// arithmetic, which calls it for 1-D fields.
+template <class C, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TF flux_1d(const StagCore<TP, TF, TC>& a, TP p_, TP pm_, TC b_,
+                                      TC bm_, TF u, TF ul, TF ur, TF am, TF a0, TF ap) {
+  static_assert(!C::HAS_V && !C::AXI, "1-D fields");
+  const TF b = (TF)b_;
+  const TF bm = (TF)bm_;
+  const TF p = (TF)p_;
+  const TF pm = (TF)pm_;
   if constexpr (C::EXACT) {
-    // a_v_p.dot(p): offsets [-s, 0] -> (0 + (-bm)*pm) + b*p
+    // a_v_p.dot(p): offsets [-1, 0] -> (0 + (-bm)*pm) + b*p
     const TF t = xadd(-xmul(bm, pm), xmul(b, p));
     if constexpr (!C::MEMORY) {
       return -t;  // heat flux: q = -a_q_t.dot(T)
     } else {
-      const TF u = sF[pos];
       TF r = t;
-      if constexpr (C::ABSORB) r = xsub(r, absorb_term<C>(a, sF, pos, i));
-      if constexpr (C::AXI && C::ABSORB && IS_X) {
-        // + dt*mu/rho * vx / r**2   (pyfds/acoustics.py:213-215)
-        const TF rad = (TF)ldg_t(a.rx + x);
-        const TF e = xmul((TF)ldg_t(a.ex + i), u);
-        r = xadd(r, e / xmul(rad, rad));
+      if constexpr (C::ABSORB) {
+        TF acc = TF(0);
+        acc = xadd(acc, xmul(am, ul));
+        acc = xadd(acc, xmul(a0, u));
+        acc = xadd(acc, xmul(ap, ur));
+        r = xsub(r, acc);
       }
       return xsub(u, r);
     }
   } else {
     if constexpr (!C::MEMORY) {
       if constexpr (sizeof(TP) > sizeof(TF)) {
-        // float64 potential, float32 flux: the difference of the two products is
-        // formed in float64 (near 300 K the float32 spacing, 2^-15 K, would swamp
-        // small gradients) and only the flux is rounded to float32
-        const TP bp = (TP)sB[pos] * sP[pos];
-        return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
+        const TP bp = (TP)b_ * p_;
+        return (TF)fma((TP)bm_, pm_, -bp);
       } else if constexpr (sizeof(TF) == 4 || std::is_same<TF, dw>::value) {
-        // float32 / double-word temperature stored as T - offset: add the reference's
-        // interface term -(b - bm) * offset (zero inside a material, and when offset
-        // is 0)
         return settle(fma(-(b - bm), (TF)a.offset, fma(bm, pm, -(b * p))));
       } else {
         return settle(fma(bm, pm, -(b * p)));
       }
     } else {
-      TF acc = sF[pos];
+      TF acc = u;
       acc = fma(-b, p, acc);
       acc = fma(bm, pm, acc);
-      if constexpr (C::ABSORB) acc = absorb_fma<C>(a, sF, pos, i, acc);
-      if constexpr (C::AXI && C::ABSORB && IS_X) {
-        const TF rad = (TF)ldg_t(a.rx + x);
-        acc = acc - ((TF)ldg_t(a.ex + i) * sF[pos]) / (rad * rad);
+      if constexpr (C::ABSORB) {
+        acc = fma(am, ul, acc);
+        acc = fma(a0, u, acc);
+        acc = fma(ap, ur, acc);
       }
       return settle(acc);
+    }
+  }
+}
+
+// New flux at flat index i from the potential slots (pos, pos - back) and the
+// old flux; sB holds this direction's factors (slots of out-of-range cells hold 0).
+template <class C, bool IS_X, typename TP, typename TF, typename TC>
+__device__ __forceinline__ TF flux_new(const StagCore<TP, TF, TC>& a, const TP* sP, const TF* sF,
+                                       const TC* sB, int pos, int64_t i, int x) {
+  if constexpr (!C::HAS_V) {
+    // 1-D fields: the same arithmetic as the warp kernel's register form
+    static_assert(IS_X, "1-D fields have x fluxes only");
+    TF u = TF(0), ul = TF(0), ur = TF(0), am = TF(0), a0 = TF(0), ap = TF(0);
+    if constexpr (C::MEMORY) u = sF[pos];
+    if constexpr (C::MEMORY && C::ABSORB) {
+      ul = sF[pos - 1];
+      ur = sF[pos + 1];
+      am = (TF)ldg0(a.axm, i - 1, a.n);
+      a0 = (TF)ldg0(a.ad, i, a.n);
+      ap = (TF)ldg0(a.axp, i + 1, a.n);
+    }
+    return flux_1d<C>(a, sP[pos], sP[pos - 1], sB[pos], sB[pos - 1], u, ul, ur, am, a0, ap);
+  } else {
+    const int back = IS_X ? 1 : C::RX;
+    const TF b = (TF)sB[pos];
+    const TF bm = (TF)sB[pos - back];
+    const TF p = (TF)sP[pos];
+    const TF pm = (TF)sP[pos - back];
+    if constexpr (C::EXACT) {
+      // a_v_p.dot(p): offsets [-s, 0] -> (0 + (-bm)*pm) + b*p
+      const TF t = xadd(-xmul(bm, pm), xmul(b, p));
+      if constexpr (!C::MEMORY) {
+        return -t;  // heat flux: q = -a_q_t.dot(T)
+      } else {
+        const TF u = sF[pos];
+        TF r = t;
+        if constexpr (C::ABSORB) r = xsub(r, absorb_term<C>(a, sF, pos, i));
+        if constexpr (C::AXI && C::ABSORB && IS_X) {
+          // + dt*mu/rho * vx / r**2   (pyfds/acoustics.py:213-215)
+          const TF rad = (TF)ldg_t(a.rx + x);
+          const TF e = xmul((TF)ldg_t(a.ex + i), u);
+          r = xadd(r, e / xmul(rad, rad));
+        }
+        return xsub(u, r);
+      }
+    } else {
+      if constexpr (!C::MEMORY) {
+        if constexpr (sizeof(TP) > sizeof(TF)) {
+          // float64 potential, float32 flux: the difference of the two products is
+          // formed in float64 (near 300 K the float32 spacing, 2^-15 K, would swamp
+          // small gradients) and only the flux is rounded to float32
+          const TP bp = (TP)sB[pos] * sP[pos];
+          return (TF)fma((TP)sB[pos - back], sP[pos - back], -bp);
+        } else if constexpr (sizeof(TF) == 4 || std::is_same<TF, dw>::value) {
+          // float32 / double-word temperature stored as T - offset: add the reference's
+          // interface term -(b - bm) * offset (zero inside a material, and when offset
+          // is 0)
+          return settle(fma(-(b - bm), (TF)a.offset, fma(bm, pm, -(b * p))));
+        } else {
+          return settle(fma(bm, pm, -(b * p)));
+        }
+      } else {
+        TF acc = sF[pos];
+        acc = fma(-b, p, acc);
+        acc = fma(bm, pm, acc);
+        if constexpr (C::ABSORB) acc = absorb_fma<C>(a, sF, pos, i, acc);
+        if constexpr (C::AXI && C::ABSORB && IS_X) {
+          const TF rad = (TF)ldg_t(a.rx + x);
+          acc = acc - ((TF)ldg_t(a.ex + i) * sF[pos]) / (rad * rad);
+        }
+        return settle(acc);
+      }
     }
   }
 }

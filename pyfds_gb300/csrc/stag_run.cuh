@@ -4,6 +4,8 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -12,6 +14,7 @@
 #include "batch_kernel.cuh"
 #include "march_kernel.cuh"
 #include "cluster_1d.cuh"
+#include "warp_1d.cuh"
 #include "resident_1d.cuh"
 #include "stag_kernel.cuh"
 
@@ -410,25 +413,38 @@ int32_t run_resident(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTab
   return FDS_OK;
 }
 
-// Every step of a call of a 1-D field spread over one thread-block cluster of `ncta`
-// CTAs (stag_1d_cluster_kernel): the prologue, then one cluster launch.
-template <class C, typename TP, typename TF, typename TC>
-int32_t run_cluster(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
-                    int64_t step0, int32_t nsteps, cudaStream_t stream, int ncta) {
-  const int n = (int)a.n;
-  const int m = (n + ncta - 1) / ncta;
-  ncta = (n + m - 1) / m;  // every CTA owns at least one cell
-  size_t smem = resident_smem<TP, TF, TC>(m) + kResidentTableBytes;
-  int64_t pool_cached = 0;
-  if (tabs->pool && tabs->pool_len > 0 &&
-      smem + (size_t)tabs->pool_len * sizeof(double) <= kResidentMaxSmem) {
-    pool_cached = tabs->pool_len;
-    smem += (size_t)pool_cached * sizeof(double);
+// Whether the device schedules one cluster of `ctas` CTAs of `kernel` (beyond the
+// portable size: the non-portable size is allowed first) with `threads` threads and
+// `smem` bytes of dynamic shared memory.
+template <typename Kernel>
+bool cluster_fits(Kernel kernel, int ctas, int threads, size_t smem) {
+  if (ctas <= kClusterPortableCta) return true;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)ctas, 1, 1);
+  cfg.blockDim = dim3((unsigned)threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess || clusters < 1) {
+    (void)cudaGetLastError();
+    return false;
   }
-  LaunchShape ls;
-  const int32_t rc =
-      kernel_shape<stag_1d_cluster_kernel<C, TP, TF, TC>>(smem, kClusterThreads, false, &ls);
-  if (rc != FDS_OK) return rc;
+  return true;
+}
+
+// The first step's potential bounds and probes of a resident 1-D run, and the state
+// pointers and step of its launch; returns FDS_OK or an error code.
+template <typename TP, typename TF, typename TC>
+int32_t resident_prologue(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
+                          int64_t step0, cudaStream_t stream) {
   const FdsCompTables& t0 = tabs->comp[0];
   if (t0.bound_tile_start || t0.probe_tile_start) {
     stag_prologue_kernel<TP><<<1, 1024, 0, stream>>>((TP*)st->cur[0], t0, tabs->pool, step0,
@@ -439,23 +455,132 @@ int32_t run_cluster(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTabl
   a.p_in = (const TP*)st->cur[0];
   a.u_in = (const TF*)st->cur[1];
   a.step = step0;
+  return FDS_OK;
+}
+
+// One launch of `kernel` as a single cluster of `ctas` CTAs.
+template <typename... Params, typename... Args>
+cudaError_t launch_cluster(void (*kernel)(Params...), int ctas, int threads, size_t smem,
+                           cudaStream_t stream, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)ctas, 1, 1);
+  cfg.blockDim = dim3((unsigned)threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Every step of a call of a 1-D field on the warps of one cluster of up to `max_ctas`
+// CTAs (stag_1d_warp_kernel, K steps per exchange block): the prologue, then one
+// cluster launch; kWaveUnsupported where the field needs more warps than that.
+template <class C, typename TP, typename TF, typename TC>
+int32_t run_warp1d(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
+                   int64_t step0, int32_t nsteps, cudaStream_t stream, int max_ctas, int want_k) {
+  const int n = (int)a.n;
+  const int K = std::min(kWarpMaxBlockSteps,
+                         std::max(1, want_k > 0 ? want_k : kWarpDefaultBlockSteps));
+  const int m = warp_owned_cells(K);
+  const int nw = (n + m - 1) / m;  // warps with cells
+  const auto kernel = stag_1d_warp_kernel<C, TP, TF, TC>;
+  int ncta = 0, nwc = 0;
+  size_t smem = 0;
+  int64_t pool_cached = 0;
+  auto shape = [&](int ctas) {
+    ncta = std::min(ctas, nw);
+    nwc = (nw + ncta - 1) / ncta;
+    ncta = (nw + nwc - 1) / nwc;
+    smem = warp_inbox_bytes<TP, TF>(nwc, K + 1) +
+           warp_slot_bytes((nwc - 1) * m + kWarpLanes) + kResidentTableBytes;
+    pool_cached = 0;
+    if (tabs->pool && tabs->pool_len > 0 &&
+        smem + (size_t)tabs->pool_len * sizeof(double) <= kResidentMaxSmem) {
+      pool_cached = tabs->pool_len;
+      smem += (size_t)pool_cached * sizeof(double);
+    }
+    return nwc <= kWarpMaxPerCta && smem <= kResidentMaxSmem;
+  };
+  if (!shape(max_ctas)) return kWaveUnsupported;
+  LaunchShape ls;
+  int32_t rc = kernel_shape<stag_1d_warp_kernel<C, TP, TF, TC>>(smem, nwc * 32, false, &ls);
+  if (rc != FDS_OK) return rc;
+  if (!cluster_fits(kernel, ncta, nwc * 32, smem)) {
+    if (!shape(std::min(max_ctas, kClusterPortableCta))) return kWaveUnsupported;
+    rc = kernel_shape<stag_1d_warp_kernel<C, TP, TF, TC>>(smem, nwc * 32, false, &ls);
+    if (rc != FDS_OK) return rc;
+  }
+  rc = resident_prologue(a, st, tabs, step0, stream);
+  if (rc != FDS_OK) return rc;
+  const bool odd = (nsteps & 1) != 0;  // the state ends where nsteps swaps leave it
+  TP* p_fin = (TP*)(odd ? st->nxt[0] : st->cur[0]);
+  TF* u_fin = (TF*)(odd ? st->nxt[1] : st->cur[1]);
+  const cudaError_t e = launch_cluster(kernel, ncta, nwc * 32, smem, stream, a, nsteps, p_fin,
+                                       u_fin, pool_cached, (int32_t)K);
+  if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "1-D warp launch: %s", cudaGetErrorString(e));
+  if (odd)
+    for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+  return FDS_OK;
+}
+
+// Every step of a call of a 1-D field on one thread-block cluster of up to `ncta` CTAs:
+// on warps with one cell per lane (stag_1d_warp_kernel) where the field fits them, else
+// on shared-memory windows (stag_1d_cluster_kernel), halo cells exchanged once per block
+// of K steps either way. Tuning overrides: FDS_CLUSTER_CTAS caps the cluster size,
+// FDS_CLUSTER_BLOCK_STEPS sets K, FDS_1D_KERNEL=window selects the window kernel.
+template <class C, typename TP, typename TF, typename TC>
+int32_t run_cluster(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTables* tabs,
+                    int64_t step0, int32_t nsteps, cudaStream_t stream, int ncta) {
+  const int n = (int)a.n;
+  const char* env_ctas = std::getenv("FDS_CLUSTER_CTAS");
+  const char* env_steps = std::getenv("FDS_CLUSTER_BLOCK_STEPS");
+  const char* env_kernel = std::getenv("FDS_1D_KERNEL");
+  const int want_k = env_steps ? std::atoi(env_steps) : 0;
+  int max_ctas = kClusterMaxCta;
+  if (env_ctas && std::atoi(env_ctas) >= 2) max_ctas = std::min(max_ctas, std::atoi(env_ctas));
+  ncta = std::min(ncta, max_ctas);
+  if (!(env_kernel && std::strcmp(env_kernel, "window") == 0)) {
+    const int32_t rw = run_warp1d<C>(a, st, tabs, step0, nsteps, stream, max_ctas, want_k);
+    if (rw != kWaveUnsupported) return rw;
+  }
+  const auto kernel = stag_1d_cluster_kernel<C, TP, TF, TC>;
+  int m = 0, K = 0;
+  size_t smem = 0;
+  int64_t pool_cached = 0;
+  auto shape = [&](int ctas) {
+    m = (n + ctas - 1) / ctas;
+    K = cluster_block_steps(m, want_k);
+    smem = cluster_inbox_bytes<TP, TF>(K + 1) + cluster_window_bytes<TP, TF, TC>(m + 2 * (K + 1)) +
+           kResidentTableBytes;
+    pool_cached = 0;
+    if (tabs->pool && tabs->pool_len > 0 &&
+        smem + (size_t)tabs->pool_len * sizeof(double) <= kResidentMaxSmem) {
+      pool_cached = tabs->pool_len;
+      smem += (size_t)pool_cached * sizeof(double);
+    }
+    return (n + m - 1) / m;  // every CTA owns at least one cell
+  };
+  ncta = shape(ncta);
+  LaunchShape ls;
+  int32_t rc = kernel_shape<stag_1d_cluster_kernel<C, TP, TF, TC>>(smem, kClusterThreads, false, &ls);
+  if (rc != FDS_OK) return rc;
+  if (!cluster_fits(kernel, ncta, kClusterThreads, smem)) {
+    ncta = shape(kClusterPortableCta);
+    rc = kernel_shape<stag_1d_cluster_kernel<C, TP, TF, TC>>(smem, kClusterThreads, false, &ls);
+    if (rc != FDS_OK) return rc;
+  }
+  rc = resident_prologue(a, st, tabs, step0, stream);
+  if (rc != FDS_OK) return rc;
   const bool odd = (nsteps & 1) != 0;
   TP* p_fin = (TP*)(odd ? st->nxt[0] : st->cur[0]);
   TF* u_fin = (TF*)(odd ? st->nxt[1] : st->cur[1]);
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)ncta, 1, 1);
-  cfg.blockDim = dim3(kClusterThreads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)ncta;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, stag_1d_cluster_kernel<C, TP, TF, TC>, a,
-                                           nsteps, p_fin, u_fin, pool_cached, (int32_t)m);
+  const cudaError_t e = launch_cluster(kernel, ncta, kClusterThreads, smem, stream, a, nsteps,
+                                       p_fin, u_fin, pool_cached, (int32_t)m, (int32_t)K);
   if (e != cudaSuccess) return set_error(FDS_E_LAUNCH, "1-D cluster launch: %s", cudaGetErrorString(e));
   if (odd)
     for (int k = 0; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
@@ -463,18 +588,25 @@ int32_t run_cluster(StagArgs<TP, TF, TC>& a, FdsStagState* st, const FdsStagTabl
 }
 
 // Cells per CTA below which a 1-D field stays in one CTA (a cluster of CTAs of at
-// least this many cells each otherwise, up to the portable cluster size)
-constexpr int kClusterMinCellsPerCta = 128;
+// least this many cells each otherwise, up to kClusterMaxCta)
+constexpr int kClusterMinCellsPerCta = 64;
+constexpr int kClusterMinCells = 256;
 
 // A 1-D field of n cells: in one cluster (ncta > 1), in one CTA (ncta == 1), or not
 // resident at all (0, one launch per step).
 template <typename TP, typename TF, typename TC>
 int resident_ctas(int64_t n) {
-  if (n >= 2 * kClusterMinCellsPerCta && n <= (int64_t)kClusterMaxCta * kClusterMaxCellsPerCta) {
+  // (up to the cells that the portable cluster size holds: run_cluster falls back to
+  // it where the device refuses a larger cluster)
+  if (n >= kClusterMinCells && n <= (int64_t)kClusterPortableCta * kClusterMaxCellsPerCta) {
     const int ncta = (int)std::min<int64_t>(kClusterMaxCta,
                                             (n + kClusterMinCellsPerCta - 1) / kClusterMinCellsPerCta);
-    const int m = (int)((n + ncta - 1) / ncta);
-    if (resident_smem<TP, TF, TC>(m) + kResidentTableBytes <= kResidentMaxSmem) return ncta;
+    const int m = (int)((n + kClusterPortableCta - 1) / kClusterPortableCta);  // the largest
+    const int g = cluster_block_steps(m, kClusterWindow) + 1;  // the widest window edge
+    if (cluster_inbox_bytes<TP, TF>(g) + cluster_window_bytes<TP, TF, TC>(m + 2 * g) +
+            kResidentTableBytes <=
+        kResidentMaxSmem)
+      return ncta;
   }
   if (n <= kResidentMaxCells && resident_smem<TP, TF, TC>((int)n) + kResidentTableBytes <= kResidentMaxSmem)
     return 1;
