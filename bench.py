@@ -361,7 +361,11 @@ def run_batched(args):
                          "traffic": _traffic_from_profiles(
                              "batched_%s%s" % (args.precision, "_tb2" if spl == 2 else "")),
                          "peak_kind": peak_kind, "kernel": "stag_batch_kernel",
-                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl},
+                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl,
+                         **({"limit": "the field stays on chip (no DRAM traffic per step): "
+                                      "the step is bound by the dependent FP64 chain, 4 DFMA "
+                                      "per step at 64 cycles each on GB300"}
+                            if resident_1d else {})},
             "clocks": clk.summary(),
             # per replay: the prologue, then one launch per step (per two with stages 3)
             "gpu_launches": int(args.steps * (runner.launches() + 1))}
@@ -955,9 +959,16 @@ def run_ours(args):
         raise RuntimeError("a kernel reported status 0x%x during the timed runs" % kernel_status)
     st_used = eng.stages()
     from pyfds_gb300 import _capi as _c
-    # a 1-D field of at most 4096 cells runs every step of a call in one launch
-    resident_1d = (args.workload != "nonlinear1d" and cells <= 4096 and st_used in (0, 4)
+    # a 1-D field of at most 8192 cells runs every step of a call in one launch: from
+    # 256 cells on the warps of a thread-block cluster (up to 4096 cells, else on
+    # shared-memory windows of a cluster), below that in one CTA
+    resident_1d = (args.workload != "nonlinear1d" and cells <= 8192 and st_used in (0, 4)
                    and not field._stag_flags() & _c.FLAG_HAS_V)
+    kernel_1d = ("stag_1d_warp_kernel (every step of the call on the warps of one "
+                 "thread-block cluster, a cell per lane)" if 256 <= cells <= 4096 else
+                 "stag_1d_cluster_kernel (every step of the call on one thread-block "
+                 "cluster)" if cells > 4096 else
+                 "stag_1d_resident_kernel (every step of the call in one CTA)")
     # steps per launch: two with two steps per tile, every step of the call for the
     # wavefront kernel (stages 4, one launch per simulate call), else one
     spl = 2 if st_used == 3 else (nt if st_used == 4 or resident_1d else 1)
@@ -1040,12 +1051,15 @@ def run_ours(args):
                                     "nonlinear1d": "nl1d_kernel (every step in one launch; the "
                                                    "field stays in L1/L2)"}.get(
                                         args.workload,
-                                        "stag_1d_resident_kernel (every step of the call "
-                                        "in one CTA)" if resident_1d else
+                                        kernel_1d if resident_1d else
                                         {3: "stag_tb2_kernel", 4: "stag_wave_kernel (every "
                                          "step of the call in one launch)"}.get(
                                             st_used, "stag_step_kernel")),
-                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl},
+                         "bytes_per_cell": bpc, "launch_ms": launch_ms, "steps_per_launch": spl,
+                         **({"limit": "the field stays on chip (no DRAM traffic per step): "
+                                      "the step is bound by the dependent FP64 chain, 4 DFMA "
+                                      "per step at 64 cycles each on GB300"}
+                            if resident_1d else {})},
             "clocks": clk.summary(),
             # per simulate(): a prologue, then per step (per two steps with stages 3)
             # the step kernel (and, for a moving medium, the row shift and the next
