@@ -989,7 +989,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for name in field._stag_components:
-            getattr(field, name).values = host_init[name].copy()
+            getattr(field, name).values = host_init[name]  # (the setter keeps a reference)
         field._coef_version += 1  # coefficients count as this step's inputs
         field.step = 0
         field.simulate(nt)

@@ -116,14 +116,19 @@ _PINNED = {"buf": None, "event": None}
 
 
 class HostUpload:
-    """Host arrays bound for many device tensors, sent in one copy.
+    """Host arrays bound for many device tensors, sent in few copies.
 
-    ``add`` records (host array, destination tensor); ``flush`` packs the arrays into
-    one pinned staging buffer (kept between calls, grown on demand), copies it to the
-    device in one transfer and then fills every destination on the device: a copy
-    with the dtype conversion the destination asks for, or for double words the
-    split of float64 values into float32 pairs (fds_dw_split). A batch of fields
-    thus pays one host-to-device transfer instead of a few per field."""
+    ``add`` records (host array, destination tensor); ``flush`` packs the small arrays
+    into one pinned staging buffer (kept between calls, grown on demand), copies it to
+    the device in one transfer and then fills every destination on the device: a copy
+    with the dtype conversion the destination asks for, or for double words the split
+    of float64 values into float32 pairs (fds_dw_split). A batch of fields thus pays
+    one host-to-device transfer instead of a few per field. Arrays of ``DIRECT_BYTES``
+    or more are copied straight from the caller's memory instead (on the GB300's Grace
+    host a pageable copy runs at 125 GB/s, while packing into the staging buffer moves
+    bytes at about 20 GB/s)."""
+
+    DIRECT_BYTES = 1 << 20
 
     def __init__(self, torch, device):
         self.torch, self.device = torch, device
@@ -141,6 +146,38 @@ class HostUpload:
         torch = self.torch
         if not self.items:
             return
+        lib = _capi.load()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        dtypes = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+                  np.dtype(np.uint8): torch.uint8}
+        small = []
+        for item in self.items:
+            off, b, dst, dword = item
+            if b.nbytes < self.DIRECT_BYTES or b.dtype not in dtypes or not b.flags.writeable:
+                small.append(item)
+                continue
+            src = torch.from_numpy(b)
+            if dword:
+                staged = torch.empty(b.size, dtype=torch.float64, device=self.device)
+                staged.copy_(src.view(-1).to(torch.float64))
+                _capi.check(lib.fds_dw_split(C.c_void_p(staged.data_ptr()),
+                                             C.c_void_p(dst.data_ptr()), b.size, stream))
+            elif dst.dtype == src.dtype:
+                dst.view(-1).copy_(src.view(-1))
+            else:
+                staged = torch.empty(b.size, dtype=src.dtype, device=self.device)
+                staged.copy_(src.view(-1))
+                dst.view(-1).copy_(staged)  # converts to dst's dtype
+        size = 0
+        packed = []
+        for _, b, dst, dword in small:
+            packed.append((size, b, dst, dword))
+            size = (size + b.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
+        self.items, self.size = packed, size
+        if not packed:
+            self.items = []
+            self.size = 0
+            return
         ev = _PINNED["event"]
         if ev is not None:
             ev.synchronize()  # the previous flush's copy has left the pinned buffer
@@ -156,10 +193,6 @@ class HostUpload:
         ev = torch.cuda.Event()
         ev.record(torch.cuda.current_stream())
         _PINNED["event"] = ev
-        lib = _capi.load()
-        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-        dtypes = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
-                  np.dtype(np.uint8): torch.uint8}
         for off, b, dst, dword in self.items:
             src = staged[off:off + b.nbytes]
             if dword:
@@ -310,11 +343,15 @@ class StagEngine:
         return v
 
     def download(self, name):
+        """The component's values as a new float64 host array: read from the device
+        into pinned memory (torch's caching host allocator; the array keeps its block)."""
+        torch = _torch()
         bufs = self.buffers[name]
-        if self.field.precision == "dw":
-            v = device_join_dw(_torch(), bufs[0]).to("cpu").numpy()
-        else:
-            v = bufs[0].detach().to("cpu").to(_torch().float64).numpy().copy()
+        src = device_join_dw(torch, bufs[0]) if self.field.precision == "dw" else bufs[0]
+        src = src.detach().reshape(-1).to(torch.float64)
+        host = torch.empty(src.numel(), dtype=torch.float64, pin_memory=True)
+        host.copy_(src)
+        v = host.numpy()
         if name == self.field._stag_components[0] and self.offset:
             v += self.offset
         return v
@@ -578,13 +615,14 @@ class StagEngine:
             comp = getattr(f, name)
             for out, c0, npts in _tables.output_column_slices(comp.outputs):
                 # one contiguous row per point: the reference's lists of float64
-                # samples are built from contiguous memory (1.5x faster than columns)
+                # samples (as Python floats: tolist is twice as fast as numpy scalars)
+                # built from contiguous memory (1.5x faster than columns)
                 rows = np.ascontiguousarray(host[:, c0:c0 + npts].T)
                 if not out.signals:
-                    out.signals = [list(r) for r in rows]
+                    out.signals = [r.tolist() for r in rows]
                 else:
                     for sig, r in zip(out.signals[:npts], rows):
-                        sig.extend(r)
+                        sig.extend(r.tolist())
         return bool(st & _capi.STATUS_NONFINITE)
 
     def report_nonfinite(self, step):
