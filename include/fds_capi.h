@@ -38,7 +38,7 @@ extern "C" {
 
 /* 3: FdsBoundGroup.primary (was padding; kernels that apply bounds to global arrays
  *    read it), FdsStagProblem.stages = 3, FDS_PREC_DW, fds_dw_split / fds_dw_join */
-#define FDS_ABI_VERSION 4
+#define FDS_ABI_VERSION 5
 
 /* error codes */
 #define FDS_OK 0
@@ -337,6 +337,34 @@ int32_t fds_stag_flow_shift(const FdsStagProblem* prob, FdsStagState* state, int
  * pyfds_gb300, done where the data already is.) */
 int32_t fds_dw_split(const double* in, void* out, int64_t n, void* stream);
 int32_t fds_dw_join(const void* in, double* out, int64_t n, void* stream);
+
+/* One array of a host gather: n float64 values at the HOST address src, written to
+ * the DEVICE address dst as float64 (FDS_GATHER_F64), float32 rounded to nearest
+ * (FDS_GATHER_F32) or double words as fds_dw_split forms them (FDS_GATHER_DW). */
+typedef struct FdsGatherItem {
+  const double* src;
+  void* dst;
+  int64_t n;
+  int32_t kind;
+  int32_t pad;
+} FdsGatherItem;
+
+#define FDS_GATHER_F64 0
+#define FDS_GATHER_F32 1
+#define FDS_GATHER_DW 2
+
+/* 1 when the current device reads pageable host memory coherently through the
+ * host's page tables (Grace-class hosts: NVLink-C2C with address translation), the
+ * condition for fds_host_gather; 0 otherwise. */
+int32_t fds_host_access(void);
+
+/* Copies `count` host arrays to the device in one kernel that reads the caller's
+ * pageable memory directly, converting each value as its item says; `items` is a
+ * HOST array of `count` items. The arrays (and `items`) must stay valid until the
+ * stream's work has finished. FDS_E_ARG where fds_host_access() is 0 or an item is
+ * malformed. (New: replaces per-array host-to-device copies, each of which waits
+ * for the stream, when a batch uploads the state and coefficients of many fields.) */
+int32_t fds_host_gather(const FdsGatherItem* items, int32_t count, void* stream);
 
 /* Workspace (device bytes, 256-byte aligned) a batched call over `count` instances
  * with `total_tiles` tiles in all needs: per-instance descriptors and the work

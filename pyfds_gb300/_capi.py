@@ -12,7 +12,7 @@ import numpy as np
 
 from ._build import LIB_PATH
 
-FDS_ABI_VERSION = 4
+FDS_ABI_VERSION = 5
 
 FDS_OK = 0
 FDS_E_ARG = -1
@@ -53,6 +53,7 @@ EXPORTED_SYMBOLS = ("fds_abi_version", "fds_last_error", "fds_stag_tile_shape",
                     "fds_stag_batch_run", "fds_selftest_bounded_wait", "fds_stag_batch_run_static",
                     "fds_stag_flow_shift",
                     "fds_nl1d_run", "fds_thermoacoustic_run", "fds_dw_split", "fds_dw_join",
+                    "fds_host_access", "fds_host_gather",
                     # include/fds_surrogate.h
                     "fds_conv3x3", "fds_conv_packed_elems", "fds_conv_pack", "fds_conv3x3_wgrad",
                     "fds_conv_wgrad_max_grid", "fds_adamw", "fds_surr_pack", "fds_surr_loss",
@@ -107,6 +108,10 @@ BOUND_OP_DTYPE = np.dtype([("scalar", "<f8"), ("mul", "<f8"), ("off", "<i8"),
 BOUND_GROUP_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("op_begin", "<i4"),
                               ("op_end", "<i4"), ("primary", "<i4")], align=True)
 PROBE_DTYPE = np.dtype([("cell", "<i8"), ("pos", "<i4"), ("col", "<i4")], align=True)
+GATHER_ITEM_DTYPE = np.dtype([("src", "<u8"), ("dst", "<u8"), ("n", "<i8"), ("kind", "<i4"),
+                              ("pad", "<i4")], align=True)
+GATHER_F64, GATHER_F32, GATHER_DW = 0, 1, 2
+assert GATHER_ITEM_DTYPE.itemsize == 32
 assert BOUND_OP_DTYPE.itemsize == 32
 assert BOUND_GROUP_DTYPE.itemsize == 24
 assert PROBE_DTYPE.itemsize == 16
@@ -226,6 +231,10 @@ def load(path=None):
     lib.fds_stag_flow_shift.restype = C.c_int32
     lib.fds_stag_flow_shift.argtypes = [C.POINTER(FdsStagProblem), C.POINTER(FdsStagState),
                                         C.c_int64, C.c_void_p]
+    lib.fds_host_access.restype = C.c_int32
+    lib.fds_host_access.argtypes = []
+    lib.fds_host_gather.restype = C.c_int32
+    lib.fds_host_gather.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
     lib.fds_dw_split.restype = C.c_int32
     lib.fds_dw_split.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     lib.fds_dw_join.restype = C.c_int32

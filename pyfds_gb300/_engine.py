@@ -115,6 +115,19 @@ class _Blob:
 _PINNED = {"buf": None, "event": None}
 
 
+_HOST_ACCESS = {}
+
+
+def _host_access():
+    """Whether the current device reads pageable host memory (fds_host_access), per
+    device."""
+    import torch
+    dev = torch.cuda.current_device()
+    if dev not in _HOST_ACCESS:
+        _HOST_ACCESS[dev] = bool(_capi.load().fds_host_access())
+    return _HOST_ACCESS[dev]
+
+
 class HostUpload:
     """Host arrays bound for many device tensors, sent in few copies.
 
@@ -124,9 +137,11 @@ class HostUpload:
     with the dtype conversion the destination asks for, or for double words the split
     of float64 values into float32 pairs (fds_dw_split). A batch of fields thus pays
     one host-to-device transfer instead of a few per field. Arrays of ``DIRECT_BYTES``
-    or more are copied straight from the caller's memory instead (on the GB300's Grace
-    host a pageable copy runs at 125 GB/s, while packing into the staging buffer moves
-    bytes at about 20 GB/s)."""
+    or more go straight from the caller's memory instead (on the GB300's Grace host a
+    pageable copy runs at 125 GB/s, while packing into the staging buffer moves bytes
+    at about 20 GB/s): where the device reads pageable host memory (fds_host_access)
+    the float64 ones in one gather kernel that converts as it writes
+    (fds_host_gather), else one copy each."""
 
     DIRECT_BYTES = 1 << 20
 
@@ -150,23 +165,58 @@ class HostUpload:
         stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         dtypes = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
                   np.dtype(np.uint8): torch.uint8}
-        small = []
+        small, direct, convert = [], [], []
+        stage_bytes = 0
         for item in self.items:
             off, b, dst, dword = item
             if b.nbytes < self.DIRECT_BYTES or b.dtype not in dtypes or not b.flags.writeable:
                 small.append(item)
-                continue
-            src = torch.from_numpy(b)
-            if dword:
-                staged = torch.empty(b.size, dtype=torch.float64, device=self.device)
-                staged.copy_(src.view(-1).to(torch.float64))
-                _capi.check(lib.fds_dw_split(C.c_void_p(staged.data_ptr()),
-                                             C.c_void_p(dst.data_ptr()), b.size, stream))
-            elif dst.dtype == src.dtype:
-                dst.view(-1).copy_(src.view(-1))
+            elif not dword and dst.dtype == dtypes[b.dtype]:
+                direct.append((b, dst, dword, None))
             else:
-                staged = torch.empty(b.size, dtype=src.dtype, device=self.device)
-                staged.copy_(src.view(-1))
+                direct.append((b, dst, dword, stage_bytes))
+                stage_bytes = (stage_bytes + b.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
+        if direct and _host_access():
+            # the device reads the float64 arrays where they are, in one kernel that
+            # converts as it writes; the stream is synchronised before the arrays (and
+            # the item table) may go
+            kinds = {torch.float64: _capi.GATHER_F64, torch.float32: _capi.GATHER_F32}
+            gather, rest, stage_bytes = [], [], 0
+            for b, dst, dword, so in direct:
+                kind = _capi.GATHER_DW if dword else kinds.get(dst.dtype)
+                if b.dtype == np.float64 and kind is not None and dst.is_contiguous():
+                    gather.append((b, dst, kind))
+                else:
+                    so = None if so is None else stage_bytes
+                    if so is not None:
+                        stage_bytes = (stage_bytes + b.nbytes + _ALIGN - 1) // _ALIGN * _ALIGN
+                    rest.append((b, dst, dword, so))
+            if gather:
+                table = np.zeros(len(gather), dtype=_capi.GATHER_ITEM_DTYPE)
+                for k, (b, dst, kind) in enumerate(gather):
+                    table[k] = (b.ctypes.data, dst.data_ptr(), b.size, kind, 0)
+                _capi.check(lib.fds_host_gather(C.c_void_p(table.ctypes.data), len(gather),
+                                                stream))
+                torch.cuda.current_stream().synchronize()
+                del table, gather
+            direct = rest
+        # arrays that the device converts land in one staging buffer first; a copy from
+        # pageable memory waits for the stream's earlier work, so all of them go before
+        # any conversion is queued
+        stage = torch.empty(stage_bytes, dtype=torch.uint8, device=self.device) if stage_bytes else None
+        for b, dst, dword, so in direct:
+            src = torch.from_numpy(b).view(-1)
+            if so is None:
+                dst.view(-1).copy_(src)
+                continue
+            staged = stage[so:so + b.nbytes].view(src.dtype)
+            staged.copy_(src)
+            convert.append((staged, dst, dword))
+        for staged, dst, dword in convert:
+            if dword:
+                _capi.check(lib.fds_dw_split(C.c_void_p(staged.data_ptr()),
+                                             C.c_void_p(dst.data_ptr()), staged.numel(), stream))
+            else:
                 dst.view(-1).copy_(staged)  # converts to dst's dtype
         size = 0
         packed = []

@@ -18,7 +18,7 @@ STRUCTS = [_capi.FdsCoefs, _capi.FdsStagProblem, _capi.FdsStagState, _capi.FdsCo
            _capi.FdsStagTables, _capi.FdsNl1dProblem, _capi.FdsConvArgs, _capi.FdsWgradArgs,
            _capi.FdsAdamArgs, _capi.FdsSurrData]
 RECORDS = {"FdsBoundOp": _capi.BOUND_OP_DTYPE, "FdsBoundGroup": _capi.BOUND_GROUP_DTYPE,
-           "FdsProbe": _capi.PROBE_DTYPE}
+           "FdsProbe": _capi.PROBE_DTYPE, "FdsGatherItem": _capi.GATHER_ITEM_DTYPE}
 
 pytestmark = pytest.mark.skipif(shutil.which("gcc") is None, reason="needs a host C compiler")
 

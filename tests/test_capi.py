@@ -103,3 +103,12 @@ def test_selftest_argument_checks(lib):
     assert lib.fds_selftest_bounded_wait(0, None, None, 10, None) == _capi.FDS_E_ARG
     assert lib.fds_selftest_bounded_wait(0, C.c_void_p(256), None, 0, None) == _capi.FDS_E_ARG
     assert lib.fds_selftest_bounded_wait(1, C.c_void_p(256), None, 10, None) == _capi.FDS_E_ARG
+
+
+def test_host_gather_argument_checks(lib):
+    """fds_host_gather rejects a negative count or a null table before any GPU work,
+    and an empty gather is a no-op."""
+    assert lib.fds_host_gather(None, -1, None) == _capi.FDS_E_ARG
+    assert lib.fds_host_gather(None, 1, None) == _capi.FDS_E_ARG
+    assert lib.fds_host_gather(None, 0, None) == _capi.FDS_OK
+    assert _capi.GATHER_ITEM_DTYPE.itemsize == 32
