@@ -1,8 +1,9 @@
 // Nonlinear 1-D acoustics (IdealGas1D, Acoustic2ndOrder1D; pyfds/nonlinear_acoustics.py).
 //
 // These grids are small (hundreds to thousands of cells) and the steps many, so every
-// step of a call runs in one cooperative launch: CTA b owns tile b (tile_x cells) and
-// loops over the steps. A step's phases (pressure bounds/outputs, velocity update and
+// step of a call runs in one launch: CTA b owns tile b (tile_x cells) and loops over
+// the steps; grids of up to 16 tiles as one thread-block cluster with hardware
+// barriers, larger ones as a cooperative launch with global-memory grid barriers. A step's phases (pressure bounds/outputs, velocity update and
 // bounds/outputs, density update and bounds/outputs, state equation) touch a
 // neighbour's cell in two places only: the velocity update reads p[i-1], the density
 // update reads v[i+1] and d[i+1]. So two grid-wide barriers per step suffice: after
@@ -114,7 +115,18 @@ __device__ bool grid_barrier(unsigned* count, unsigned k) {
   return __syncthreads_and(ok) != 0;
 }
 
-template <bool EXACT, int KIND, bool CONV, bool NLS>
+// Every thread of every CTA of the cluster arrives; the release / acquire pair at
+// cluster scope orders each CTA's global-memory writes before the barrier with the
+// other CTAs' reads after it.
+__device__ __forceinline__ void nl_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n"
+               "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// CLUSTER: the grid is one thread-block cluster (up to 16 CTAs) and the step's two
+// barriers are the hardware cluster barrier (about a tenth of the global-memory grid
+// barrier's cost); else a cooperative launch with bounded grid barriers.
+template <bool EXACT, int KIND, bool CONV, bool NLS, bool CLUSTER>
 __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
   using O = Ops<EXACT>;
   const int n = a.n;
@@ -133,7 +145,12 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
     apply_bounds<EXACT>(a.tab[0], t, p, a.pool, step);
     __syncthreads();
     write_probes(a.tab[0], t, p, a.row0 + s);
-    if (!grid_barrier(a.sync, k++)) break;
+    if constexpr (CLUSTER) {
+      nl_cluster_sync();
+      ++k;
+    } else if (!grid_barrier(a.sync, k++)) {
+      break;
+    }
     // velocity: v - ((a_v_p p) / B [+ a_v_v2 v] - (a_v_v v) / B), B = rho0 + d
     for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       double t1 = 0.0;  // backward difference: diagonals -1 (-f1) then 0 (f1)
@@ -158,7 +175,12 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
     apply_bounds<EXACT>(a.tab[1], t, vn, a.pool, step);
     __syncthreads();
     write_probes(a.tab[1], t, vn, a.row0 + s);
-    if (!grid_barrier(a.sync, k++)) break;
+    if constexpr (CLUSTER) {
+      nl_cluster_sync();
+      ++k;
+    } else if (!grid_barrier(a.sync, k++)) {
+      break;
+    }
     // density: d - a_d_v ((d + rho0) v), forward difference: diagonals 0 (-f1), +1 (f1)
     for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
       const double w0 = O::mul(O::add(r[i], a.rho0[i]), vn[i]);
@@ -195,15 +217,41 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
 
 using NlKernel = void (*)(NlArgs);
 
-template <bool EXACT>
+template <bool EXACT, bool CLUSTER>
 NlKernel pick(int kind, bool conv, bool nls) {
   if (kind == FDS_NL1D_IDEAL_GAS) {
-    if (conv && nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, true>;
-    if (conv) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, false>;
-    if (nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, true>;
-    return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, false>;
+    if (conv && nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, true, CLUSTER>;
+    if (conv) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, true, false, CLUSTER>;
+    if (nls) return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, true, CLUSTER>;
+    return nl1d_kernel<EXACT, FDS_NL1D_IDEAL_GAS, false, false, CLUSTER>;
   }
-  return nl1d_kernel<EXACT, FDS_NL1D_SECOND_ORDER, true, false>;
+  return nl1d_kernel<EXACT, FDS_NL1D_SECOND_ORDER, true, false, CLUSTER>;
+}
+
+constexpr int kNlMaxClusterCta = 16;  // with the non-portable cluster size allowed
+
+// Whether one cluster of `ctas` CTAs of `fn` (threads each, no dynamic shared memory)
+// can be scheduled: the portable size always, up to 16 where the device allows it.
+bool nl_cluster_fits(NlKernel fn, int ctas, int threads) {
+  if (ctas > kNlMaxClusterCta) return false;
+  if (ctas <= 8) return true;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)ctas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)ctas, 1, 1);
+  cfg.blockDim = dim3((unsigned)threads, 1, 1);
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess || clusters < 1) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return true;
 }
 
 }  // namespace
@@ -254,9 +302,35 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
   a.nsteps = nsteps;
   const bool conv = prob->kind == FDS_NL1D_SECOND_ORDER || (prob->flags & FDS_NL1D_CONVECTIVE);
   const bool nls = (prob->flags & FDS_NL1D_NL_STATE) != 0;
-  NlKernel fn = (prob->flags & FDS_FLAG_EXACT) ? pick<true>(prob->kind, conv, nls)
-                                               : pick<false>(prob->kind, conv, nls);
+  const bool exact = (prob->flags & FDS_FLAG_EXACT) != 0;
   const int threads = prob->tile_x < 256 ? ((prob->tile_x + 31) / 32) * 32 : 256;
+  cudaStream_t s = (cudaStream_t)stream;
+  // a grid of at most 16 tiles: one cluster, every step in one launch with hardware
+  // barriers (no barrier counter, no per-launch step limit)
+  NlKernel fc = exact ? pick<true, true>(prob->kind, conv, nls) : pick<false, true>(prob->kind, conv, nls);
+  if (nl_cluster_fits(fc, ntiles, threads)) {
+    a.step0 = step0;
+    a.row0 = 0;
+    a.nsteps = nsteps;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)ntiles;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)ntiles, 1, 1);
+    cfg.blockDim = dim3((unsigned)threads, 1, 1);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fc, a);
+    if (e != cudaSuccess)
+      return set_error(FDS_E_LAUNCH, "nonlinear 1-D cluster launch: %s", cudaGetErrorString(e));
+    if (nsteps & 1)
+      for (int k = 1; k < 3; ++k) std::swap(st->cur[k], st->nxt[k]);
+    return FDS_OK;
+  }
+  NlKernel fn = exact ? pick<true, false>(prob->kind, conv, nls) : pick<false, false>(prob->kind, conv, nls);
   // every CTA waits for the others at the grid barriers: all must be resident
   int dev = 0, sms = 0, per_sm = 0, coop = 0;
   cudaError_t q = cudaGetDevice(&dev);
@@ -269,7 +343,6 @@ extern "C" int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* st,
   if (!coop || (int64_t)per_sm * sms < ntiles)
     return set_error(FDS_E_SIZE, "%d tiles cannot all be resident (%d per SM x %d SMs)", ntiles,
                      per_sm, sms);
-  cudaStream_t s = (cudaStream_t)stream;
   for (int64_t done = 0; done < nsteps;) {
     const int32_t m = (int32_t)std::min<int64_t>(per_launch, nsteps - done);
     a.step0 = step0 + done;
