@@ -985,18 +985,25 @@ def run_ours(args):
     for o in (field.pressure.outputs if hasattr(field, "pressure") else []):
         o.signals = []
     h2d = d2h = 0
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_call():
         for name in field._stag_components:
             getattr(field, name).values = host_init[name]  # (the setter keeps a reference)
         field._coef_version += 1  # coefficients count as this step's inputs
         field.step = 0
         field.simulate(nt)
         pot = getattr(field, field._stag_components[0])
-        result = pot.values  # device -> host read of the final potential
+        out = pot.values  # device -> host read of the final potential
         for o in pot.outputs:
             o.signals = []
+        return out
+
+    if e2e_steps:
+        e2e_call()  # untimed: the first call compiles the tables and warms the allocators
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        result = e2e_call()
     barrier()
     e2e_s = (time.perf_counter() - t0) / max(e2e_steps, 1)
     if not e2e_steps:
