@@ -448,16 +448,24 @@ def test_coupled_fields_vs_reference(gpu, exact):
         compare(S2.coupled_results(obj, kind_of), g, prefix, check)
 
 
-@pytest.mark.parametrize("variant", ["thermoacoustic", "thermoacoustic3"])
-def test_thermoacoustic_native_equals_step_by_step(gpu, variant, monkeypatch):
+@pytest.mark.parametrize("variant,nx,block", [("thermoacoustic", 45, "0"),
+                                              ("thermoacoustic3", 45, "0"),
+                                              ("thermoacoustic", 1000, "1"),
+                                              ("thermoacoustic3", 1000, "3"),
+                                              ("thermoacoustic3", 777, "8")])
+def test_thermoacoustic_native_equals_step_by_step(gpu, variant, nx, block, monkeypatch):
     """ThermoAcoustic1D's one-call stepping (fds_thermoacoustic_run) against the
     reference's loop (fields stepped one by one, coupling applied on the host), both
     exact; simulate is split into two chunks so that an accumulated transfer crosses
-    a call boundary."""
+    a call boundary. One-call stepping runs every step of a call in one launch on the
+    warps of a cluster, exchanging window edges every K steps (FDS_CLUSTER_BLOCK_STEPS;
+    0: the default): the 45-cell cases on 3 CTAs of one warp, the 777- and 1000-cell
+    cases on 8 warps per CTA."""
     import pyfds_gb300
     from coupled_helpers import kind_of
     from oracle import scenarios as S2
-    spec = S2.coupled_scenario(77, variant, nx=45, steps=27)
+    monkeypatch.setenv("FDS_CLUSTER_BLOCK_STEPS", block)
+    spec = S2.coupled_scenario(77, variant, nx=nx, steps=27)
     a = S2.build_coupled(pyfds_gb300, spec, build_field, exact=True)
     assert a._native_path()
     a.simulate(7)
