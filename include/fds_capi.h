@@ -316,7 +316,10 @@ int32_t fds_nl1d_run(const FdsNl1dProblem* prob, FdsStagState* state,
  *   step and, when step % stepping == 0, T += acc and acc is emptied; otherwise
  *   T += loss when step % stepping == 0.
  * acc: [n] device accumulator; *acc_empty (host, in/out) says it holds nothing yet.
- * Both problems must be float64 1-D fields of the same size. */
+ * Both problems must be float64 1-D fields of the same size. Fields of up to 2048
+ * cells (with both in exact mode or both not) run every step of the call in one
+ * launch on a thread-block cluster; the results are the per-step launches' bit for
+ * bit. */
 int32_t fds_thermoacoustic_run(const FdsStagProblem* acoustic, FdsStagState* ac_state,
                                const FdsStagTables* ac_tables, const FdsStagProblem* thermal,
                                FdsStagState* th_state, const FdsStagTables* th_tables,
