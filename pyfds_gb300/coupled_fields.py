@@ -87,8 +87,8 @@ class ThermoAcoustic1D(cp.SynchronizedFields):
         torch = require_cuda()
         acf, thf = self.fields
         ea, et = acf._engine(), thf._engine()
-        pa = ea.prepare(step0, n)
-        pt = et.prepare(step0, n)
+        pa = ea.prepare(step0, n, cache_tables=True)
+        pt = et.prepare(step0, n, cache_tables=True)
         dev = ea.coef_tensors["bx"].device
         key = (acf._coef_version, thf._coef_version)
         if self._coupling_vectors is None or self._coupling_vectors[0] != key:

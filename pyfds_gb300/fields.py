@@ -84,7 +84,9 @@ class Field:
                 edges = sorted({int(round(num_steps * k / 20)) for k in range(21)})
                 chunks = [b - a for a, b in zip(edges[:-1], edges[1:]) if b > a]
             for n in chunks:
-                diverged = self._engine().run(self.step, n)
+                # tables are reused while the boundaries, outputs and tiling are
+                # unchanged (a fingerprint with content checksums) and cover the steps
+                diverged = self._engine().run(self.step, n, cache_tables=True)
                 if progress_logger:
                     progress_logger.log(self.step + n - 1)
                 self.step += n
