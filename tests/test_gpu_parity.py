@@ -452,7 +452,8 @@ def test_coupled_fields_vs_reference(gpu, exact):
                                               ("thermoacoustic3", 45, "0"),
                                               ("thermoacoustic", 1000, "1"),
                                               ("thermoacoustic3", 1000, "3"),
-                                              ("thermoacoustic3", 777, "8")])
+                                              ("thermoacoustic3", 777, "8"),
+                                              ("thermoacoustic3", 2100, "0")])
 def test_thermoacoustic_native_equals_step_by_step(gpu, variant, nx, block, monkeypatch):
     """ThermoAcoustic1D's one-call stepping (fds_thermoacoustic_run) against the
     reference's loop (fields stepped one by one, coupling applied on the host), both
@@ -460,7 +461,8 @@ def test_thermoacoustic_native_equals_step_by_step(gpu, variant, nx, block, monk
     a call boundary. One-call stepping runs every step of a call in one launch on the
     warps of a cluster, exchanging window edges every K steps (FDS_CLUSTER_BLOCK_STEPS;
     0: the default): the 45-cell cases on 3 CTAs of one warp, the 777- and 1000-cell
-    cases on 8 warps per CTA."""
+    cases on 8 warps per CTA; 2100 cells exceed a cluster's warps and step with one
+    launch per field and step plus a loss kernel."""
     import pyfds_gb300
     from coupled_helpers import kind_of
     from oracle import scenarios as S2
