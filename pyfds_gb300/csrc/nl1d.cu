@@ -161,14 +161,17 @@ __global__ void __launch_bounds__(256) nl1d_kernel(const NlArgs a) {
       t3 = O::add(t3, O::mul(O::mul(-2.0, a.a[i]), v[i]));
       if (i + 1 < n) t3 = O::add(t3, O::mul(a.a[i + 1], v[i + 1]));
       const double B = O::add(a.rho0[i], r[i]);
-      double term = O::div(t1, B);
+      // exact: the reference's two divisions; otherwise one reciprocal of B (each
+      // quotient within an ulp or so of the division's, inside the 1e-12 bar)
+      const double rB = EXACT ? 0.0 : __drcp_rn(B);
+      double term = EXACT ? O::div(t1, B) : t1 * rB;
       if (CONV) {
         double t2 = 0.0;  // central difference: diagonals -1 (-fc) then +1 (fc)
         if (i >= 1) t2 = O::add(t2, O::mul(-fc, v[i - 1]));
         if (i + 1 < n) t2 = O::add(t2, O::mul(fc, v[i + 1]));
         term = O::add(term, t2);
       }
-      term = O::sub(term, O::div(t3, B));
+      term = O::sub(term, EXACT ? O::div(t3, B) : t3 * rB);
       vn[i] = O::sub(v[i], term);
     }
     __syncthreads();
