@@ -569,14 +569,20 @@ class StagEngine:
         geo = self._geometry(batched)
         step_end = step0 + nsteps
         if cache_tables:
-            # the tables depend on the tiling too (tile shape, slot layout)
+            # the tables depend on the tiling too (tile shape, slot layout); they serve
+            # every call that ends within the signals (a call past them recompiles,
+            # which raises the reference's error for a signal that is too short)
             fp = (self._fingerprint(), geo.tx, geo.ty, geo.layout)
             if self.table_cache is not None and self.table_cache[0] == fp and \
                     self.table_cache[2] >= step_end:
                 tabs = self.table_cache[1]
             else:
                 tabs = self._compile_tables(torch, dev, max(step_end, 1), geo, up)
-                self.table_cache = (fp, tabs, step_end)
+                covered = [_tables.signal_steps(getattr(f, name).boundaries)
+                           for name in f._stag_components]
+                covered = [c for c in covered if c is not None]
+                self.table_cache = (fp, tabs, max(step_end, min(covered)) if covered
+                                    else float("inf"))
         else:
             tabs = self._compile_tables(torch, dev, step_end, geo, up)
         outs = [torch.empty((nsteps, max(nc, 1)), dtype=torch.float64, device=dev)

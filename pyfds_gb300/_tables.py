@@ -271,6 +271,25 @@ def _boundary_ops(b, n, pool, step_end):
     return cells, ops
 
 
+def signal_steps(boundaries):
+    """Steps the signal values of a boundary list cover (the shortest signal's length;
+    None without signals): tables compiled from them serve every step range ending
+    there, the pool holding each signal whole."""
+    best = None
+    for b in boundaries:
+        value = b.value
+        if np.ndim(value) == 0:
+            continue
+        if isinstance(value, np.ndarray):
+            length = value.shape[0] if value.ndim >= 1 else None
+        else:
+            lengths = [len(sig) for sig in value if np.ndim(sig) == 1]
+            length = min(lengths) if lengths else None
+        if length is not None:
+            best = length if best is None else min(best, length)
+    return best
+
+
 def compile_bounds(boundaries, n, pool, step_end, geo, role, offset=0.0):
     """Group/op/tile tables of one component's boundary list (None if empty).
 
