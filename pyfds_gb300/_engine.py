@@ -670,15 +670,10 @@ class StagEngine:
                 host = host + self.offset
             comp = getattr(f, name)
             for out, c0, npts in _tables.output_column_slices(comp.outputs):
-                # one contiguous row per point: the reference's lists of float64
-                # samples (as Python floats: tolist is twice as fast as numpy scalars)
-                # built from contiguous memory (1.5x faster than columns)
-                rows = np.ascontiguousarray(host[:, c0:c0 + npts].T)
-                if not out.signals:
-                    out.signals = [r.tolist() for r in rows]
-                else:
-                    for sig, r in zip(out.signals[:npts], rows):
-                        sig.extend(r.tolist())
+                # one contiguous row per point; the reference's lists of float64
+                # samples (Python floats: tolist is twice as fast as numpy scalars)
+                # are built from it when Output.signals is read
+                out._record(np.ascontiguousarray(host[:, c0:c0 + npts].T))
         return bool(st & _capi.STATUS_NONFINITE)
 
     def report_nonfinite(self, step):

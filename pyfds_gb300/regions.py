@@ -90,12 +90,44 @@ class Boundary:
 class Output:
     """Values recorded from a component every step (pyfds/regions.py:148-165).
 
-    ``signals[k]`` is the list of samples of the k-th point of the region.
+    ``signals[k]`` is the list of samples of the k-th point of the region. The
+    samples a GPU call records arrive as a float64 block on the host; lists that
+    exist grow at once, new ones are built when ``signals`` is next read (building
+    Python lists of millions of samples costs more than the call's copy; a caller
+    that never reads them does not pay for it).
     """
 
     def __init__(self, region):
         self.region = region
-        self.signals = []
+        self._signals = []
+        self._pending = []  # host blocks [points, steps] not yet in the lists
+
+    @property
+    def signals(self):
+        if self._pending:
+            pending, self._pending = self._pending, []
+            for rows in pending:
+                if not self._signals:
+                    self._signals = [r.tolist() for r in rows]
+                else:
+                    for sig, r in zip(self._signals[:len(rows)], rows):
+                        sig.extend(r.tolist())
+        return self._signals
+
+    @signals.setter
+    def signals(self, value):
+        self._pending = []
+        self._signals = value
+
+    def _record(self, rows):
+        """Append the samples of a GPU call: one row per point, as in ``signals``.
+        Lists that exist grow in place at once (a caller may hold them); new ones
+        are built when ``signals`` is read."""
+        if self._signals:
+            for sig, r in zip(self._signals[:len(rows)], rows):
+                sig.extend(r.tolist())
+        else:
+            self._pending.append(rows)
 
     @property
     def mean_signal(self):

@@ -94,3 +94,23 @@ def test_name(module, name):
 def test_fixture_covers_the_reference_modules():
     assert set(SURFACE) == set(IN_SCOPE) | set(OUT_OF_SCOPE)
     assert sum(len(SURFACE[m]["names"]) for m in IN_SCOPE) >= 30
+
+
+def test_output_blocks_become_lists():
+    """Samples recorded by GPU calls (Output._record) read as the reference's lists:
+    new lists when first read, lists that exist (and references to them) grow in
+    place, a reset drops what was not read."""
+    import numpy as np
+    from pyfds_gb300 import regions
+    o = regions.Output(regions.Region([1, 2], "out"))
+    o._record(np.array([[1.0, 2.0], [3.0, 4.0]]))
+    o._record(np.array([[5.0], [6.0]]))
+    assert o.signals == [[1.0, 2.0, 5.0], [3.0, 4.0, 6.0]]
+    held = o.signals[0]
+    o._record(np.array([[7.0], [8.0]]))
+    assert held == [1.0, 2.0, 5.0, 7.0]
+    assert o.signals[1] == [3.0, 4.0, 6.0, 8.0]
+    o.signals = []
+    o._record(np.array([[9.0], [10.0]]))
+    o.signals = []
+    assert o.signals == []
