@@ -225,13 +225,20 @@ __global__ void __launch_bounds__(kWarpMaxPerCta * 32, 1)
   double* const oF = (cF >= 0) ? a.tab[1].out + cF : nullptr;
   const int64_t sP = a.tab[0].ncols, sF = a.tab[1].ncols;
   const int32_t rP = a.tab[0].out_rows, rF = a.tab[1].out_rows;
-  // the step loop of a warp: without boundary cells or probes; with fast chains and
-  // single probes only, in straight-line code (a branch in the loop costs tens of
-  // cycles of the step's few hundred); or with table chains or several probes on a cell
+  // the step loop of a warp: without boundary cells or probes; with the potential's
+  // one-operation chains and single probes, in straight-line code holding only the
+  // parts the warp has (a branch, or code run for lanes that need none of it, costs
+  // tens of cycles of the step's few hundred on the dependent chain); or any other
+  // case (the general loop)
   const bool special =
       __any_sync(0xffffffffu, bP.kind != 0 || bF.kind != 0 || cP != -1 || cF != -1);
   const WarpBounds wP = warp_bounds(bP), wF = warp_bounds(bF);
-  const bool general = wP.table || wF.table || __any_sync(0xffffffffu, cP == -2 || cF == -2);
+  // straight-line loops cover the potential's one-operation chains and single
+  // probes; the flux's chains or probes, table chains and several probes on a cell
+  // take the general loop
+  const bool general = wP.table || wF.table || wF.fast ||
+                       __any_sync(0xffffffffu, cP == -2 || cF != -1);
+  const bool pprobe = __any_sync(0xffffffffu, cP != -1);
   // every CTA of the cluster runs before a neighbour writes into its shared memory
   cluster_sync();
   int blk = 0;
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(kWarpMaxPerCta * 32, 1)
       const int ke = min(K, nsteps - s0);
       // one step: new flux (its boundary chain and probes), new potential (the next
       // step's boundary chain and probes; the last step's are the next call's prologue)
-#define FDS_WARP_STEPS(MODE, ADDF, ADDP)                                               \
+#define FDS_WARP_STEPS(MODE, PB, PP, ADDP)                                             \
   for (int kk = 0; kk < ke; ++kk) {                                                    \
     const int32_t s = s0 + kk;                                                         \
     const TP pm = shfl_up1(p);                                                         \
@@ -265,11 +272,7 @@ __global__ void __launch_bounds__(kWarpMaxPerCta * 32, 1)
       ur = shfl_down1(u);                                                              \
     }                                                                                  \
     TF un = flux_1d<C>(a, p, pm, b, bm, u, ul, ur, am, a0, ap);                        \
-    if constexpr (MODE == 1) {                                                         \
-      if constexpr (std::is_same<TF, double>::value)                                   \
-        un = lane_bound<ADDF>(bF, un, a.step + s);                                     \
-      if (oF && s < rF) oF[s * sF] = (double)un;                                       \
-    } else if constexpr (MODE == 2) {                                                  \
+    if constexpr (MODE == 2) {                                                         \
       if constexpr (std::is_same<TF, double>::value)                                   \
         if (wF.fast) un = lane_bound<true>(bF, un, a.step + s);                        \
       if (wF.table && bF.kind == 1) un = bound_chain(rt[1], bF.range, un, pool, a.step + s); \
@@ -280,9 +283,10 @@ __global__ void __launch_bounds__(kWarpMaxPerCta * 32, 1)
     TP pn = potential_regs<C>(a, p, u, un1, TF(0), TF(0), k, kn, TF(0), TF(0), cell);  \
     if constexpr (MODE == 1) {                                                         \
       const bool next = s + 1 < nsteps;                                                \
-      if constexpr (std::is_same<TP, double>::value)                                   \
+      if constexpr (PB && std::is_same<TP, double>::value)                             \
         pn = next ? lane_bound<ADDP>(bP, pn, a.step + s + 1) : pn;                     \
-      if (oP && next && s + 1 < rP) oP[(s + 1) * sP] = (double)pn;                     \
+      if constexpr (PP)                                                                \
+        if (oP && next && s + 1 < rP) oP[(s + 1) * sP] = (double)pn;                   \
     } else if constexpr (MODE == 2) {                                                  \
       if (s + 1 < nsteps) {                                                            \
         if constexpr (std::is_same<TP, double>::value)                                 \
@@ -295,15 +299,21 @@ __global__ void __launch_bounds__(kWarpMaxPerCta * 32, 1)
     if (in) p = pn;                                                                    \
   }
       if (!special) {
-        FDS_WARP_STEPS(0, false, false)
+        FDS_WARP_STEPS(0, false, false, false)
       } else if (general) {
-        FDS_WARP_STEPS(2, true, true)
-      } else if (!wF.add && !wP.add) {
-        FDS_WARP_STEPS(1, false, false)
-      } else if (!wF.add) {
-        FDS_WARP_STEPS(1, false, true)
+        FDS_WARP_STEPS(2, false, false, false)
+      } else if (!wP.fast) {
+        FDS_WARP_STEPS(1, false, true, false)
+      } else if (!pprobe) {
+        if (wP.add) {
+          FDS_WARP_STEPS(1, true, false, true)
+        } else {
+          FDS_WARP_STEPS(1, true, false, false)
+        }
+      } else if (wP.add) {
+        FDS_WARP_STEPS(1, true, true, true)
       } else {
-        FDS_WARP_STEPS(1, true, true)
+        FDS_WARP_STEPS(1, true, true, false)
       }
 #undef FDS_WARP_STEPS
     }
