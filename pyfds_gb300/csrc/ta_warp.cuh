@@ -73,15 +73,17 @@ __device__ __forceinline__ TaLane ta_lane(const ResidentTables& rt, const FdsCom
 }
 
 // The chain and probe of one component for step `step` / output row `row`: MODE 0 none,
-// 1 one-operation chains (straight-line, the addition for the warp) and single probes,
-// 2 any (table chains, several probes on a cell).
+// 1 one-operation chains and single probes, 2 any (table chains, several probes on a
+// cell).
 template <int MODE>
 __device__ __forceinline__ double ta_apply(const TaLane& l, const WarpBounds& w,
                                            const ResidentTables& rt, const FdsCompTables& tb,
                                            const double* pool, double v, int64_t step,
                                            int64_t row, int cell) {
   if constexpr (MODE == 1) {
-    v = lane_bound<true>(l.b, v, step);
+    // a uniform branch skips the components without chains in this warp (running the
+    // chain code on every lane would cost more than the branch)
+    if (w.fast) v = lane_bound<true>(l.b, v, step);
     if (l.out && row < l.rows) l.out[row * l.stride] = v;
   } else if constexpr (MODE == 2) {
     if (w.fast) v = lane_bound<true>(l.b, v, step);
