@@ -246,3 +246,16 @@ def test_kernel_model_fuzz():
             assert np.array_equal(st_o[c], st_m[c]), (case, c)
             for a, b in zip(sg_o[c], sg_m[c]):
                 assert np.array_equal(a, b), (case, c)
+
+
+def test_signal_steps_bounds_table_reuse():
+    """Compiled tables serve every call that ends within the shortest signal of the
+    boundaries (signal_steps); scalar values do not limit them."""
+    from pyfds_gb300 import regions as R
+    from pyfds_gb300._tables import signal_steps
+    reg = R.Region([1, 2], "b")
+    assert signal_steps([R.Boundary(reg, value=3.0)]) is None
+    assert signal_steps([R.Boundary(reg, value=np.zeros(50)),
+                         R.Boundary(reg, value=np.zeros((40, 2)))]) == 40
+    assert signal_steps([R.Boundary(reg, value=[np.zeros(30), np.zeros(35)]),
+                         R.Boundary(reg, value=1.0)]) == 30
