@@ -203,7 +203,7 @@ def _boundary_ops(b, n, pool, step_end):
     npts = idx.size
     value = b.value
     mul = float(b.additive)
-    if np.ndim(value) == 0:
+    if np.ndim(value) == 0:  # (ragged per-point signals raise here, as in the reference)
         kind = "scalar"
     elif isinstance(value, np.ndarray):
         kind = "array%d" % value.ndim
@@ -278,10 +278,13 @@ def signal_steps(boundaries):
     best = None
     for b in boundaries:
         value = b.value
-        if np.ndim(value) == 0:
+        if isinstance(value, (list, tuple)):
+            lengths = [len(sig) for sig in value if np.ndim(sig) == 1]
+            length = min(lengths) if lengths else None
+        elif np.ndim(value) == 0:
             continue
-        if isinstance(value, np.ndarray):
-            length = value.shape[0] if value.ndim >= 1 else None
+        elif isinstance(value, np.ndarray):
+            length = value.shape[0]
         else:
             lengths = [len(sig) for sig in value if np.ndim(sig) == 1]
             length = min(lengths) if lengths else None
